@@ -1,0 +1,423 @@
+#!/usr/bin/env python3
+"""Throughput benchmark: D3Q19 MLUPS of the fused stream-collide step and its HBM roofline.
+
+Workload (default): 512x256x256 channel (z streamwise) packed with seeded non-overlapping spheres
+of radius U[4,12] to porosity 0.7, periodic in x/y, Zou-He-style velocity inlet u_z=0.04 at z=0
+and pressure outlet rho=1 at z=255, Re=200 on the mean sphere diameter, BGK + Smagorinsky
+(cs=0.1), FP64 populations.  Inputs (10.2 GB of populations) are far larger than L2, so no L2
+flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  `value` is device-timed (CUDA events around K graph-launched
+steps on the engine's stream); `e2e` times the same metric through the C ABI from Python: the
+lattice is uploaded from host arrays, each step is a tlbm_step call, and every 100 steps the
+seven output fields of write_data are read back to host memory.  `cpu_baseline` times the CPU
+restatement of the reference's timestep (oracle/, array-of-structures push with an int32
+neighbour table, OpenMP over nodes) on the host cores on a slab of the same geometry.
+"""
+
+from __future__ import annotations
+
+import argparse
+import hashlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "D3Q19 MLUPS (% HBM roofline); BF16/learned vs plain FP64 at equal L2 error"
+CPU_SAMPLE_NZ = 32
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=30)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--lattice", default="D3Q19")
+    ap.add_argument("--precision", default="f64", choices=["f64", "f32", "bf16", "f16"])
+    ap.add_argument("--arithmetic", default="fast", choices=["fast", "reference"])
+    ap.add_argument("--nx", type=int, default=512)
+    ap.add_argument("--ny", type=int, default=256)
+    ap.add_argument("--nz", type=int, default=256)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--no-extras", action="store_true", help="skip e2e, CPU and extra lines")
+    return ap.parse_args()
+
+
+# ----------------------------------------------------------------------------- distributed
+
+
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ----------------------------------------------------------------------------- workload
+
+
+def workload(args):
+    from tlbm_gb300 import geometry as G
+
+    key = "%d_%d_%d_%d" % (args.nx, args.ny, args.nz, args.seed)
+    cache = os.path.join("/tmp", "tlbm_bench_geom_%s.npz" % hashlib.md5(key.encode()).hexdigest())
+    if os.path.exists(cache):
+        z = np.load(cache)
+        g = G.Geometry(args.nx, args.ny, args.nz, z["nd"])
+        g.meta = json.loads(str(z["meta"]))
+        g.lo = g.meta["mean_diameter"]
+    else:
+        g = G.random_sphere_pack(args.nx, args.ny, args.nz, 4.0, 12.0, 0.7, seed=args.seed,
+                                 max_tries=3_000_000)
+        try:
+            np.savez(cache, nd=g.nd_type.astype(np.int8), meta=json.dumps(g.meta))
+        except OSError:
+            pass
+    g.nd_type = g.nd_type.astype(np.int32)
+    p = G.params_lattice_units(g, args.lattice, 0.04, 200.0, g.lo, args.steps, cs=0.1,
+                               rho_lbm=1.0, plot_freq=100)
+    return g, p
+
+
+def cpu_sample(g, p):
+    """A z-slab of the workload for the CPU baseline: first CPU_SAMPLE_NZ planes of the pack,
+    inlet plane kept, last plane turned into the outlet."""
+    nz = min(CPU_SAMPLE_NZ, g.nz)
+    nd = g.nd_type.reshape(g.nz, g.ny, g.nx)[:nz].copy()
+    nd[-1][nd[-1] != 1] = 3
+    return nd.reshape(-1), nz
+
+
+# ----------------------------------------------------------------------------- clocks
+
+
+class ClockSampler:
+    """nvidia-smi samples every 200 ms while running (read-only queries)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+        time.sleep(0.3)
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [s.strip() for s in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                if int(parts[0]) != self.index:
+                    continue
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {
+            "sm_mhz": statistics.median(sm) if sm else None,
+            "sm_max_mhz": max(smax) if smax else None,
+            "power_w_max": max(power) if power else None,
+            "samples": len(sm),
+            "reasons": sorted(reasons),
+        }
+
+
+# ----------------------------------------------------------------------------- roofline
+
+
+def peaks():
+    path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_cell(lattice, precision):
+    """DRAM bytes per cell-update of the step kernel from the committed ncu summary, if any."""
+    path = os.path.join(HERE, "profiles", "traffic.json")
+    if not os.path.exists(path):
+        return None
+    d = json.load(open(path))
+    v = d.get("%s_%s" % (lattice, precision))
+    return None if v is None else float(v["dram_bytes_per_cell"])
+
+
+# ----------------------------------------------------------------------------- arms
+
+
+def cpu_baseline(g, p, steps=20, warmup=2):
+    sys.path.insert(0, os.path.join(HERE, "tests"))
+    import oracle_lib
+
+    nd, nz = cpu_sample(g, p)
+    q = int(p.lattice[3:])
+    threads = os.cpu_count() or 1
+    o = oracle_lib.Oracle(q, 1, p.cs, p.rho_lbm, p.u_lbm, p.omega, g.nx, g.ny, nz, nd,
+                          prec="f64", threads=threads)
+    o.run(warmup)
+    t0 = time.perf_counter()
+    o.run(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    cells = g.nx * g.ny * nz
+    return {
+        "value": round(cells * steps / dt / 1e6, 3),
+        "unit": "MLUPS",
+        "cores": threads,
+        "kind": "port",
+        "sample": "%dx%dx%d slab of the same sphere pack (%s FP64 BGK+Smagorinsky), %d warm-up + "
+                  "%d timed steps of the C restatement of the reference timestep "
+                  "(AoS push, int32 neighbour table), OpenMP over nodes"
+                  % (g.nx, g.ny, nz, p.lattice, warmup, steps),
+    }
+
+
+def run_ours(args, dist):
+    import tlbm_gb300 as T
+    from tlbm_gb300 import build as B
+
+    B.build()
+    g, p = workload(args)
+    n = g.num_nodes
+    q = int(args.lattice[3:])
+    prob = T.problem_from_params(p)
+    part = T.TLBMPartition.from_arrays(prob, g.nd_type, precision=args.precision,
+                                       arithmetic=args.arithmetic, device=dist.local)
+    part.run(0, args.warmup)
+    part.synchronize()
+    dist.barrier()
+    part.synchronize()
+    clocks = ClockSampler(dist.local)
+    clocks.start()
+    l0 = part.kernel_launches()
+    ms = part.time_steps(args.warmup, args.steps)
+    launches = part.kernel_launches() - l0
+    clock = clocks.stop()
+    part.synchronize()
+    dist.barrier()
+    ms_max = dist.max(ms)
+    mass = part.mass()
+    part.close()
+
+    sb = {"f64": 8, "f32": 4, "bf16": 2, "f16": 2}[args.precision]
+    bytes_per_cell = 2 * q * sb + 1
+    step_s = ms_max / 1e3 / args.steps
+    value = n * args.steps * dist.world / (ms_max / 1e3) / 1e6
+    peak, peak_kind = peaks()
+    achieved = n * bytes_per_cell / step_s / 1e9
+    tpc = traffic_per_cell(args.lattice, args.precision)
+    out = {
+        "metric": METRIC,
+        "value": round(value, 2),
+        "unit": "MLUPS",
+        "n_gpus": dist.world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_max / args.steps, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": {"f64": "f64", "f32": "f32", "bf16": "bf16-storage/f32", "f16":
+                  "f16-storage/f32"}[args.precision],
+        "data": "synthetic",
+        "config": {
+            "workload": "%dx%dx%d sphere-packed channel, %s BGK+Smagorinsky cs=0.1, %s %s "
+                        "arithmetic" % (args.nx, args.ny, args.nz, args.lattice, args.precision,
+                                        args.arithmetic),
+            "cells": n,
+            "porosity": round(g.meta.get("porosity", 0.0), 5),
+            "spheres": g.meta.get("n_spheres"),
+            "re": 200.0,
+            "u_in": 0.04,
+            "omega": round(p.omega, 6),
+            "l2": "populations (%.1f GB) larger than L2; no flush" % (2 * q * sb * n / 1e9),
+            "parallelism": "replicas only" if dist.world > 1 else "single GPU",
+        },
+        "roofline": {
+            "bound": "hbm",
+            "achieved": round(achieved, 1),
+            "peak": peak,
+            "unit": "GB/s",
+            "frac": round(achieved / peak, 4),
+            "peak_kind": peak_kind,
+            "bytes_per_cell": bytes_per_cell,
+            "traffic": None if tpc is None else round(tpc * n),
+        },
+        "gpu_launches": launches,
+        "clocks": clock,
+        "final_mass": mass,
+    }
+    if not args.no_extras:
+        out["e2e"] = e2e(args, g, p, dist)
+        if dist.rank == 0 and dist.world == 1:
+            out["cpu_baseline"] = cpu_baseline(g, p)
+    return out
+
+
+def e2e(args, g, p, dist, plot_every=100):
+    """Same metric end to end through the C ABI from host buffers: upload the lattice, step with
+    one tlbm_step call per step, read the write_data fields back every `plot_every` steps."""
+    import tlbm_gb300 as T
+
+    n = g.num_nodes
+    steps = args.steps
+    dist.barrier()
+    t0 = time.perf_counter()
+    part = T.TLBMPartition.from_arrays(T.problem_from_params(p), g.nd_type,
+                                       precision=args.precision, arithmetic=args.arithmetic,
+                                       device=dist.local)
+    d2h = 0
+    for ts in range(steps):
+        part.take_LBM_time_step(ts % 2)
+        if (ts + 1) % plot_every == 0:
+            fields = part.macros() + part.force()
+            d2h += sum(a.nbytes for a in fields)
+    part.synchronize()
+    dt = time.perf_counter() - t0
+    part.close()
+    dt = dist.max(dt)
+    return {
+        "value": round(n * steps * dist.world / dt / 1e6, 2),
+        "unit": "MLUPS",
+        "h2d_bytes_per_step": round(n * 4 / steps),
+        "d2h_bytes_per_step": round(d2h / steps),
+        "includes": "lattice upload (int32 node types) + %d tlbm_step calls + write_data "
+                    "fields read back every %d steps" % (steps, plot_every),
+    }
+
+
+def run_reference(args, dist):
+    """The reference's CPU timestep (its C restatement in oracle/; the reference's own build
+    needs the reference sources, which are not available at run time) on all host cores."""
+    g, p = workload(args)
+    sys.path.insert(0, os.path.join(HERE, "tests"))
+    import oracle_lib
+
+    nd, nz = cpu_sample(g, p)
+    q = int(args.lattice[3:])
+    threads = os.cpu_count() or 1
+    o = oracle_lib.Oracle(q, 1, p.cs, p.rho_lbm, p.u_lbm, p.omega, g.nx, g.ny, nz, nd,
+                          prec="f64", threads=threads)
+    o.run(args.warmup)
+    t0 = time.perf_counter()
+    o.run(args.steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    cells = g.nx * g.ny * nz
+    value = cells * args.steps / dt / 1e6
+    sample = ("%dx%dx%d slab of the %dx%dx%d sphere pack per step, FP64 BGK+Smagorinsky, C "
+              "restatement of the reference timestep, OpenMP over nodes"
+              % (g.nx, g.ny, nz, g.nx, g.ny, g.nz))
+    return {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": round(value, 3),
+        "unit": "MLUPS",
+        "n_gpus": dist.world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(dt * 1e3 / args.steps, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "%dx%dx%d sphere-packed channel, %s BGK+Smagorinsky cs=0.1, f64"
+                               % (args.nx, args.ny, args.nz, args.lattice)},
+        "cpu_baseline": {"value": round(value, 3), "unit": "MLUPS", "cores": threads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": round(value, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            if dist.rank == 0:
+                print(json.dumps(run_reference(args, dist)), flush=True)
+            return
+        out = run_ours(args, dist)
+        if dist.rank == 0:
+            print(json.dumps(out), flush=True)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,189 @@
+/*
+ * tlbm.h -- C ABI of the GB300 lattice-Boltzmann engine.
+ *
+ * Drop-in boundary for the timestep path of stu314159/tLBM.  The reference exposes that path as
+ * the C++ class TLBM_Partition (include/TLBM_Partition.h:33-133), driven by main() in
+ * src/tLBM.cpp:7-88.  Each entry point below names the reference member it replaces.
+ *
+ * Conventions
+ *   - Every call returns a tlbm_status (0 = success); no C++ exception crosses the ABI.  After a
+ *     failure, tlbm_get_last_error() describes it.  The reference throws (runtime_error,
+ *     invalid_argument, const char*) or aborts; here the same conditions return a status.
+ *   - A handle owns all device memory and one CUDA stream.  Use one host thread per handle.
+ *   - Like the reference, inputs are the text files params.lbm, ndType.lbm and parts.lbm in the
+ *     working directory, and outputs are raw *.b_dat files written in partition-major order
+ *     (MPI_File_write_at semantics: files are created, never truncated).
+ *   - The whole lattice lives on one GPU.  A multi-partition parts.lbm only changes the order of
+ *     the output files, exactly as the reference's per-rank writes at writeOffset would.
+ *   - Output files hold the precision's output type: double for TLBM_PREC_F64, float otherwise
+ *     (the reference writes its compile-time `real`, float by default).
+ */
+#ifndef TLBM_GB300_H
+#define TLBM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int tlbm_status;
+enum {
+  TLBM_OK = 0,
+  TLBM_ERR_IO = 1,               /* a file could not be opened, read or written */
+  TLBM_ERR_INVALID_ARGUMENT = 2, /* bad argument, unknown lattice string, bad option */
+  TLBM_ERR_FORMAT = 3,           /* malformed params.lbm / ndType.lbm / parts.lbm */
+  TLBM_ERR_OUT_OF_RANGE = 4,     /* partition id >= size, node type not in {0,1,2,3,5} */
+  TLBM_ERR_CUDA = 5,             /* a CUDA runtime call or kernel launch failed */
+  TLBM_ERR_NUMERIC = 6,          /* non-finite mass detected by the FP64 watchdog */
+  TLBM_ERR_UNSUPPORTED = 7,      /* feature not available in this build / precision */
+  TLBM_ERR_TIMEOUT = 8,          /* a bounded device-side wait gave up */
+  TLBM_ERR_NO_MEMORY = 9         /* host or device allocation failed */
+};
+
+/* Storage precision of the populations (the reference's compile-time `real`,
+ * include/TLBM_definitions.h:11, as a run-time choice). */
+typedef enum {
+  TLBM_PREC_F64 = 0,  /* double populations, double arithmetic */
+  TLBM_PREC_F32 = 1,  /* float populations, float arithmetic (the reference default) */
+  TLBM_PREC_BF16 = 2, /* bfloat16 storage of f_i - w_i, float collision */
+  TLBM_PREC_F16 = 3   /* half storage of f_i - w_i, float collision */
+} tlbm_precision;
+
+/* Arithmetic flavour for TLBM_PREC_F64 / TLBM_PREC_F32. */
+typedef enum {
+  TLBM_ARITH_REFERENCE = 0, /* the reference's operation order and type promotions, no FMA
+                               contraction: bit-identical to the CPU reference */
+  TLBM_ARITH_FAST = 1       /* reassociated, FMA-contracted: same physics, not bit-identical */
+} tlbm_arith;
+
+typedef enum {
+  TLBM_CLOSURE_PARAMS = 0, /* BGK; Smagorinsky iff cs > 0 (src/TLBM_Partition.cpp:785-792) */
+  TLBM_CLOSURE_MLP = 1     /* learned eddy-viscosity closure (weights via tlbm_set_closure_mlp) */
+} tlbm_closure;
+
+typedef struct tlbm_options {
+  int struct_size; /* sizeof(tlbm_options); lets the struct grow without breaking callers */
+  int precision;   /* tlbm_precision */
+  int arithmetic;  /* tlbm_arith */
+  int closure;     /* tlbm_closure */
+  int block_x;     /* threads per block along x; 0 = tuned by the engine */
+  int block_y;     /* threads per block along y; 0 = tuned by the engine */
+  int device;      /* CUDA device ordinal */
+  int reserved[9];
+} tlbm_options;
+
+/* The 23 values of params.lbm in file order (Problem, include/Problem.h:18-40). */
+typedef struct tlbm_problem {
+  char lattice[8]; /* "D3Q15" | "D3Q19" | "D3Q27" */
+  int dynamics;    /* 1 = LBGK, 2 = stream without relaxation (reference behaviour) */
+  int num_ts, ts_rep_freq, warmup_ts, plot_freq;
+  double cs, rho_lbm, u_lbm, omega;
+  int nx, ny, nz;
+  int restart_flag, time_avg_flag;
+  double lx_p, ly_p, lz_p, t_conv, l_conv, p_conv;
+  int p_ref_idx, ss_data_flag;
+} tlbm_problem;
+
+typedef struct tlbm_handle tlbm_handle;
+
+/* Fills *opt with defaults: TLBM_PREC_F32, TLBM_ARITH_REFERENCE, TLBM_CLOSURE_PARAMS. */
+void tlbm_default_options(tlbm_options* opt);
+
+/* Replaces TLBM_Partition(int rank, int size, MPI_Comm) (include/TLBM_Partition.h:37,
+ * src/TLBM_Partition.cpp:10-14, :77-118): reads params.lbm, ndType.lbm and parts.lbm from
+ * `workdir`, builds the lattice on the GPU, writes ordering.b_dat.  `rank` must be 0 (one
+ * process drives the whole lattice); `size` must exceed the largest partition id, as the
+ * reference requires (src/TLBM_Partition.cpp:218-224).  Options: defaults, overridden by an
+ * optional `tlbm.cfg` in workdir (lines `key value`: precision f64|f32|bf16|f16,
+ * arithmetic reference|fast, block_x N, block_y N, device N). */
+tlbm_status tlbm_create(const char* workdir, int rank, int size, tlbm_handle** out);
+
+/* As tlbm_create with explicit options (tlbm.cfg is not read). */
+tlbm_status tlbm_create_ex(const char* workdir, int rank, int size, const tlbm_options* opt,
+                           tlbm_handle** out);
+
+/* In-memory inputs instead of files: `nd_type` and `parts` (may be NULL = one partition) hold
+ * nx*ny*nz values in global order g = x + y*nx + z*nx*ny.  Outputs go to `workdir` (may be
+ * NULL: no ordering.b_dat is written and tlbm_write_data fails with TLBM_ERR_IO). */
+tlbm_status tlbm_create_from_arrays(const tlbm_problem* prob, const int32_t* nd_type,
+                                    const int32_t* parts, const char* workdir,
+                                    const tlbm_options* opt, tlbm_handle** out);
+
+/* Replaces ~TLBM_Partition (src/TLBM_Partition.cpp:16-45). */
+tlbm_status tlbm_destroy(tlbm_handle* h);
+
+/* Replaces take_LBM_time_step(bool isEven) (src/TLBM_Partition.cpp:910-947): one fused
+ * stream-collide launch.  Call with is_even = ts % 2 as main() does (src/tLBM.cpp:53). */
+tlbm_status tlbm_step(tlbm_handle* h, int is_even);
+
+/* nsteps calls of take_LBM_time_step(ts % 2) for ts = first_ts .. first_ts+nsteps-1, issued as
+ * one CUDA graph launch per call (no host work between steps). */
+tlbm_status tlbm_run(tlbm_handle* h, int first_ts, int nsteps);
+
+/* As tlbm_run, timed on the handle's stream with CUDA events; *ms = device time. */
+tlbm_status tlbm_time_steps(tlbm_handle* h, int first_ts, int nsteps, float* ms);
+
+/* Waits until every step enqueued on the handle's stream has finished; returns the first
+ * asynchronous error (a step launch returns before the GPU has run it). */
+tlbm_status tlbm_synchronize(tlbm_handle* h);
+
+/* Replaces write_data() (src/TLBM_Partition.cpp:608-683): writes ux{n}, uy{n}, uz{n},
+ * density{n}, Fx{n}, Fy{n}, Fz{n}.b_dat for dump n = 0, 1, ... with the macroscopic values of
+ * the last step and the momentum-exchange force on the post-stream populations. */
+tlbm_status tlbm_write_data(tlbm_handle* h);
+
+/* Replaces write_time_avg_data() (src/TLBM_Partition.cpp:564-606): uAvg, vAvg, wAvg, rhoAvg
+ * hold sums over all steps taken (requires time_avg_flag = 1 in params.lbm). */
+tlbm_status tlbm_write_time_avg_data(tlbm_handle* h);
+
+/* Getters of TLBM_Partition (include/TLBM_Partition.h:43-50). */
+int tlbm_get_num_ts(const tlbm_handle* h);
+int tlbm_get_ts_rep_freq(const tlbm_handle* h);
+int tlbm_get_plot_freq(const tlbm_handle* h);
+int tlbm_get_warmup_ts(const tlbm_handle* h);
+int tlbm_get_num_global_nodes(const tlbm_handle* h);
+int tlbm_get_time_avg_flag(const tlbm_handle* h);
+int tlbm_is_restart(const tlbm_handle* h);
+/* Number of (node, speed) links that cross partitions of parts.lbm (get_cut_size, :685-689):
+ * what the reference would send between ranks per step; nothing is sent here. */
+int tlbm_get_cut_size(const tlbm_handle* h);
+
+/* Message for the last failure on `h` (or the last failure of a create call when h is NULL). */
+const char* tlbm_get_last_error(const tlbm_handle* h);
+const char* tlbm_status_string(tlbm_status s);
+
+/* ---- inspection (tools and tests; not part of the reference surface) ---------------------- */
+
+/* Bytes per value of output files and of the copy_* buffers below (8 or 4). */
+int tlbm_output_bytes(const tlbm_handle* h);
+int tlbm_num_speeds(const tlbm_handle* h);
+
+/* Macroscopic ux, uy, uz, rho of the last step in global node order (any pointer may be NULL). */
+tlbm_status tlbm_copy_macros(tlbm_handle* h, void* ux, void* uy, void* uz, void* rho);
+
+/* Force of calc_force (src/TLBM_Partition.cpp:174-208) on the last step, global order. */
+tlbm_status tlbm_copy_force(tlbm_handle* h, void* fx, void* fy, void* fz);
+
+/* Populations in the reference's layout f[node*Q + speed] (getIDx, include/TLBM_Partition.h:57):
+ * which = 0: after streaming (the reference's fOut); which = 1: after collision, before
+ * streaming (the reference's fIn at the end of a step). */
+tlbm_status tlbm_copy_populations(tlbm_handle* h, int which, void* out);
+
+/* Neighbour table adj[node*Q + speed] = periodic push target (create_adj_matrix,
+ * src/TLBM_Partition.cpp:254-271), computed on the GPU from the same index arithmetic the
+ * stream step uses. */
+tlbm_status tlbm_copy_adjacency(tlbm_handle* h, int32_t* out);
+
+/* Total mass sum_{node,speed} f as a deterministic FP64 reduction on the GPU. */
+tlbm_status tlbm_mass(tlbm_handle* h, double* mass);
+
+/* Number of kernels this handle has launched since creation. */
+int64_t tlbm_kernel_launches(const tlbm_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TLBM_GB300_H */

@@ -1,0 +1,153 @@
+"""The C-ABI library without a GPU: it loads, exports every function include/tlbm.h declares,
+and rejects malformed inputs (which it checks before touching the device) with the right
+status -- the conditions where the reference throws or aborts."""
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import tlbm_gb300 as T
+from tlbm_gb300 import build as B
+from tlbm_gb300 import geometry as G
+
+
+@pytest.fixture(scope="session")
+def lib():
+    B.build()
+    return T.library()
+
+
+def test_exports_every_declared_symbol(lib):
+    declared = T.declared_symbols()
+    assert len(declared) >= 25
+    out = subprocess.run(["nm", "-D", "--defined-only", B.LIB], capture_output=True, text=True,
+                         check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    missing = [s for s in declared if s not in exported]
+    assert not missing, missing
+    for s in declared:
+        assert hasattr(lib, s)
+
+
+def test_status_strings(lib):
+    assert lib.tlbm_status_string(T.OK) == b"ok"
+    assert lib.tlbm_status_string(T.ERR_FORMAT) == b"malformed input"
+
+
+def test_default_options(lib):
+    o = T.Options()
+    lib.tlbm_default_options(ctypes.byref(o))
+    assert o.struct_size == ctypes.sizeof(T.Options)
+    assert o.precision == T.PREC["f32"] and o.arithmetic == 0
+
+
+def small_inputs(tmp, lattice="D3Q19", nd=None, parts=None):
+    g = G.sphere_in_box(8, 8, 12, 2, 4, 4, 5)
+    if nd is not None:
+        g.nd_type = nd
+    p = G.params_lattice_units(g, lattice, 0.05, 20.0, 4.0, 10)
+    G.write_inputs(str(tmp), g, p, parts)
+    return g, p
+
+
+def create_status(lib, workdir, rank=0, size=1):
+    h = ctypes.c_void_p()
+    st = lib.tlbm_create(str(workdir).encode(), rank, size, ctypes.byref(h))
+    return st, lib.tlbm_get_last_error(None).decode()
+
+
+def test_missing_params(lib, tmp_path):
+    st, msg = create_status(lib, tmp_path)
+    assert st == T.ERR_IO and "params.lbm" in msg
+
+
+def test_invalid_lattice(lib, tmp_path):
+    small_inputs(tmp_path)
+    txt = open(tmp_path / "params.lbm").read().replace("D3Q19", "D3Q13")
+    open(tmp_path / "params.lbm", "w").write(txt)
+    st, msg = create_status(lib, tmp_path)
+    assert st == T.ERR_INVALID_ARGUMENT and "Invalid Lattice Structure" in msg
+
+
+def test_malformed_params(lib, tmp_path):
+    small_inputs(tmp_path)
+    lines = open(tmp_path / "params.lbm").read().splitlines(True)
+    lines[2] = "lots \n"
+    open(tmp_path / "params.lbm", "w").write("".join(lines))
+    st, msg = create_status(lib, tmp_path)
+    assert st == T.ERR_FORMAT
+
+
+def test_truncated_params(lib, tmp_path):
+    small_inputs(tmp_path)
+    lines = open(tmp_path / "params.lbm").read().splitlines(True)
+    open(tmp_path / "params.lbm", "w").write("".join(lines[:10]))
+    st, msg = create_status(lib, tmp_path)
+    assert st == T.ERR_FORMAT and "15" in msg
+
+
+def test_ndtype_wrong_length(lib, tmp_path):
+    small_inputs(tmp_path)
+    with open(tmp_path / "ndType.lbm", "a") as fh:
+        fh.write("0 \n")
+    st, msg = create_status(lib, tmp_path)
+    assert st == T.ERR_FORMAT and "ndType.lbm" in msg
+    small_inputs(tmp_path)
+    lines = open(tmp_path / "ndType.lbm").read().splitlines(True)
+    open(tmp_path / "ndType.lbm", "w").write("".join(lines[:-5]))
+    st, msg = create_status(lib, tmp_path)
+    assert st == T.ERR_FORMAT
+
+
+def test_ndtype_bad_code(lib, tmp_path):
+    g = G.sphere_in_box(8, 8, 12, 2, 4, 4, 5)
+    nd = g.nd_type.copy()
+    nd[17] = 4
+    small_inputs(tmp_path, nd=nd)
+    st, msg = create_status(lib, tmp_path)
+    assert st == T.ERR_OUT_OF_RANGE and "type 4" in msg
+
+
+def test_parts_beyond_job_size(lib, tmp_path):
+    parts = G.partition_1d(8, 8, 12, 3)
+    small_inputs(tmp_path, parts=parts)
+    st, msg = create_status(lib, tmp_path, size=2)
+    assert st == T.ERR_OUT_OF_RANGE and "partition 2" in msg
+
+
+def test_rank_must_be_zero(lib, tmp_path):
+    small_inputs(tmp_path)
+    st, msg = create_status(lib, tmp_path, rank=1)
+    assert st == T.ERR_INVALID_ARGUMENT
+
+
+def test_bad_config_file(lib, tmp_path):
+    small_inputs(tmp_path)
+    open(tmp_path / "tlbm.cfg", "w").write("precision f128\n")
+    st, msg = create_status(lib, tmp_path)
+    assert st == T.ERR_INVALID_ARGUMENT and "precision" in msg
+
+
+def test_bad_options_struct(lib, tmp_path):
+    small_inputs(tmp_path)
+    o = T.Options()
+    lib.tlbm_default_options(ctypes.byref(o))
+    o.struct_size = 3
+    h = ctypes.c_void_p()
+    st = lib.tlbm_create_ex(str(tmp_path).encode(), 0, 1, ctypes.byref(o), ctypes.byref(h))
+    assert st == T.ERR_INVALID_ARGUMENT
+
+
+def test_null_handle_calls(lib):
+    assert lib.tlbm_step(None, 0) == T.ERR_INVALID_ARGUMENT
+    assert lib.tlbm_get_num_ts(None) == -1
+    assert lib.tlbm_destroy(None) == T.ERR_INVALID_ARGUMENT
+
+
+def test_python_mirror_raises(lib, tmp_path):
+    with pytest.raises(T.TLBMError) as e:
+        T.TLBMPartition(str(tmp_path))
+    assert e.value.status == T.ERR_IO

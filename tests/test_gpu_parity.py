@@ -1,0 +1,232 @@
+"""GPU parity: the CUDA engine through the C ABI against the reference's outputs and the oracle.
+
+* reference arithmetic (FP64 and FP32): every output file byte-identical to the reference's
+  (SHA-256 digests in tests/golden), small cases and the 2000-step 32x32x128 channel;
+* neighbour table, populations, force and time averages equal the oracle bit for bit;
+* fast arithmetic: FP64 within 1e-12 (field-relative) of the reference after 2000 steps,
+  FP32 / BF16 / FP16 within the error budgets stated in each test.
+"""
+
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle_lib
+import tlbm_gb300 as T
+from cases_util import (CASES, FIELDS, SMALL, output_digests, params_tokens, rel_inf, rel_l2,
+                        write_case_inputs)
+from conftest import golden_arrays
+from tlbm_gb300 import build as B
+from tlbm_gb300 import geometry as G
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    B.build()
+    T.library()
+
+
+def run_case(name, workdir, precision, arithmetic="reference"):
+    write_case_inputs(name, workdir)
+    part = T.TLBMPartition(workdir, precision=precision, arithmetic=arithmetic)
+    T.run_like_tlbmexec(part)
+    part.synchronize()
+    return part
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+@pytest.mark.parametrize("name", SMALL)
+def test_reference_arithmetic_files_bit_exact(name, prec, tmp_path):
+    part = run_case(name, str(tmp_path), prec)
+    part.close()
+    want = CASES[name]["outputs"][prec]
+    got = output_digests(str(tmp_path))
+    assert sorted(got) == sorted(want)
+    bad = sorted(f for f in want if got[f] != want[f])
+    assert not bad, "GPU output differs from the reference in %s" % bad
+
+
+def test_channel32_2000_steps_fp64_bit_exact(tmp_path):
+    """The 32x32x128 sphere channel, D3Q19 BGK FP64, 2000 steps: byte-identical dumps."""
+    run_case("channel32_q19_2000", str(tmp_path), "f64").close()
+    want = CASES["channel32_q19_2000"]["outputs"]["f64"]
+    got = output_digests(str(tmp_path))
+    for f, h in want.items():
+        assert got[f] == h, f
+
+
+def test_tlbmexec_cli_fp32_bit_exact(tmp_path):
+    """The tLBMexec command line (reference default precision) writes the reference's files."""
+    write_case_inputs("q19_sphere_smag", str(tmp_path))
+    r = subprocess.run([B.EXE], cwd=str(tmp_path), capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert "Estimated LPU/s" in r.stdout and "Test complete." in r.stdout
+    want = CASES["q19_sphere_smag"]["outputs"]["f32"]
+    got = output_digests(str(tmp_path))
+    for f, h in want.items():
+        assert got[f] == h, f
+
+
+def fast_vs_reference(name, prec, tmp_path, steps=None):
+    spec = CASES[name]["spec"]
+    d_ref = os.path.join(str(tmp_path), "ref")
+    d_fast = os.path.join(str(tmp_path), "fast")
+    write_case_inputs(name, d_ref)
+    write_case_inputs(name, d_fast)
+    steps = steps or spec["num_ts"]
+    out = []
+    for d, p, a in ((d_ref, "f64", "reference"), (d_fast, prec, "fast")):
+        part = T.TLBMPartition(d, precision=p, arithmetic=a)
+        part.run(0, steps)
+        out.append(part.macros())
+        part.close()
+    return out
+
+
+def test_fast_fp64_channel32_2000_within_1e12(tmp_path):
+    ref, fast = fast_vs_reference("channel32_q19_2000", "f64", tmp_path)
+    for fn, a, b in zip(("ux", "uy", "uz", "rho"), fast, ref):
+        err = rel_inf(a, b)
+        assert err <= 1e-12, (fn, err)
+
+
+@pytest.mark.parametrize("name", ["q19_sphere_smag", "q27_sphere_smag", "q15_sphere_smag",
+                                  "q19_periodic_bgk", "q27_sphere_bgk"])
+def test_fast_fp64_small_within_1e12(name, tmp_path):
+    ref, fast = fast_vs_reference(name, "f64", tmp_path)
+    for fn, a, b in zip(("ux", "uy", "uz", "rho"), fast, ref):
+        assert rel_inf(a, b) <= 1e-12, fn
+
+
+@pytest.mark.parametrize("prec,tol", [("f32", 1e-4), ("f16", 2e-2), ("bf16", 1e-1)])
+def test_reduced_precision_velocity_error(prec, tol, tmp_path):
+    """Velocity-magnitude relative L2 error against FP64 after 2000 steps of the channel."""
+    ref, fast = fast_vs_reference("channel32_q19_2000", prec, tmp_path)
+    umag = lambda m: np.sqrt(m[0].astype(np.float64) ** 2 + m[1] ** 2 + m[2] ** 2)
+    err = rel_l2(umag(fast), umag(ref))
+    print("%s velocity L2 error vs FP64: %.3e" % (prec, err))
+    assert err <= tol
+    assert rel_inf(fast[3], ref[3]) <= 10 * tol
+
+
+def small_problem(q, nx=7, ny=5, nz=6, types=None, cs=0.0, time_avg=0, seed=0):
+    rng = np.random.default_rng(seed)
+    n = nx * ny * nz
+    if types is None:
+        types = rng.choice([0, 0, 0, 0, 1, 2, 3], size=n).astype(np.int32)
+    geom = G.Geometry(nx, ny, nz, types)
+    p = G.params_lattice_units(geom, "D3Q%d" % q, 0.04, 30.0, 3.0, 40, cs=cs, time_avg=time_avg)
+    return geom, p
+
+
+@pytest.mark.parametrize("q", [15, 19, 27])
+def test_adjacency_matches_oracle(q):
+    geom, p = small_problem(q)
+    part = T.TLBMPartition.from_arrays(T.problem_from_params(p), geom.nd_type, precision="f64")
+    o = oracle_lib.Oracle(q, 1, p.cs, p.rho_lbm, p.u_lbm, p.omega, geom.nx, geom.ny, geom.nz,
+                          geom.nd_type)
+    assert np.array_equal(part.adjacency(), o.adjacency())
+
+
+@pytest.mark.parametrize("q", [15, 19, 27])
+@pytest.mark.parametrize("cs", [0.0, 0.1])
+def test_populations_force_timeavg_bit_exact(q, cs):
+    """Random node types (fluid, solid, inlet, outlet) on a periodic box: after 9 steps the
+    post-stream and post-collision populations, macroscopic fields and force equal the oracle's
+    bit for bit (FP64 reference arithmetic)."""
+    geom, p = small_problem(q, cs=cs, time_avg=1, seed=q)
+    part = T.TLBMPartition.from_arrays(T.problem_from_params(p), geom.nd_type, precision="f64")
+    o = oracle_lib.Oracle(q, 1, p.cs, p.rho_lbm, p.u_lbm, p.omega, geom.nx, geom.ny, geom.nz,
+                          geom.nd_type, time_avg=1)
+    for ts in range(9):
+        part.take_LBM_time_step(ts % 2)
+    o.run(9)
+    assert np.array_equal(part.populations(0), o.populations(0))
+    assert np.array_equal(part.populations(1), o.populations(1))
+    for a, b in zip(part.macros(), o.macros()):
+        assert np.array_equal(a, b)
+    for a, b in zip(part.force(), o.force()):
+        assert np.array_equal(a, b)
+
+
+def test_time_average_files_match_oracle(tmp_path):
+    geom, p = small_problem(19, nx=9, ny=7, nz=11, time_avg=1, seed=5)
+    p.num_ts, p.plot_freq = 30, 10
+    d1, d2 = str(tmp_path / "gpu"), str(tmp_path / "cpu")
+    G.write_inputs(d1, geom, p)
+    G.write_inputs(d2, geom, p)
+    part = T.TLBMPartition(d1, precision="f64", arithmetic="reference")
+    T.run_like_tlbmexec(part)
+    part.close()
+    oracle_lib.run_dir(d2, "f64")
+    g, c = output_digests(d1), output_digests(d2)
+    assert "uAvg.b_dat" in g and sorted(g) == sorted(c)
+    assert g == c
+
+
+def test_multi_partition_output_order(tmp_path):
+    """A 3-partition parts.lbm (1D z-slabs and a 3D block split) changes only the file order:
+    ordering.b_dat and every dump equal the oracle's partition-major files."""
+    for name, parts_fn in (("z", lambda g: G.partition_1d(g.nx, g.ny, g.nz, 3)),
+                           ("b", lambda g: G.partition_geometric(g.nx, g.ny, g.nz, 2, 2, 2))):
+        geom, p = small_problem(19, nx=8, ny=6, nz=10, seed=7)
+        p.num_ts, p.plot_freq = 12, 6
+        parts = parts_fn(geom)
+        d1, d2 = str(tmp_path / (name + "gpu")), str(tmp_path / (name + "cpu"))
+        G.write_inputs(d1, geom, p, parts)
+        G.write_inputs(d2, geom, p, parts)
+        part = T.TLBMPartition(d1, size=8, precision="f64", arithmetic="reference")
+        assert part.get_cut_size() > 0
+        T.run_like_tlbmexec(part)
+        part.close()
+        oracle_lib.run_dir(d2, "f64")
+        assert output_digests(d1) == output_digests(d2)
+        order = np.fromfile(os.path.join(d1, "ordering.b_dat"), dtype=np.int32)
+        assert not np.array_equal(order, np.arange(geom.num_nodes))
+
+
+def test_graph_run_equals_single_steps():
+    geom, p = small_problem(27, nx=33, ny=9, nz=12, cs=0.1, seed=11)
+    a = T.TLBMPartition.from_arrays(T.problem_from_params(p), geom.nd_type, precision="f64")
+    b = T.TLBMPartition.from_arrays(T.problem_from_params(p), geom.nd_type, precision="f64")
+    for ts in range(13):
+        a.take_LBM_time_step(ts % 2)
+    b.run(0, 7)
+    b.run(7, 6)
+    assert np.array_equal(a.populations(0), b.populations(0))
+    assert b.kernel_launches() >= 13
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32", "bf16", "f16"])
+def test_mass_reduction(prec):
+    """FP64 mass of all populations: equals a host sum of the exported populations, is
+    deterministic, and is conserved on a closed periodic box without boundaries.  D3Q27: its
+    double-literal weights sum to 1 (the D3Q15/D3Q19 float-literal weights sum to 1 + 1.5e-8,
+    so those lattices gain mass by design, in the reference too)."""
+    geom, p = small_problem(27, nx=40, ny=24, nz=16, types=np.zeros(40 * 24 * 16, np.int32))
+    part = T.TLBMPartition.from_arrays(T.problem_from_params(p), geom.nd_type, precision=prec)
+    m0 = part.mass()
+    part.run(0, 20)
+    m1 = part.mass()
+    assert m1 == part.mass()
+    host = part.populations(1).astype(np.float64).sum()
+    assert abs(m1 - host) <= 1e-12 * abs(host) + (1e-3 if prec in ("bf16", "f16") else 0)
+    tol = {"f64": 1e-13, "f32": 1e-5, "bf16": 1e-2, "f16": 1e-3}[prec]
+    assert abs(m1 - m0) <= tol * m0
+
+
+def test_diverged_run_reports_numeric_error():
+    """The FP64 mass watchdog turns a blown-up run into TLBM_ERR_NUMERIC (omega far outside the
+    stable range makes the populations overflow within a few hundred steps)."""
+    geom, p = small_problem(19, nx=16, ny=8, nz=8, seed=2)
+    p.omega = 2.6
+    part = T.TLBMPartition.from_arrays(T.problem_from_params(p), geom.nd_type, precision="f32",
+                                       arithmetic="fast")
+    part.run(0, 3000)
+    with pytest.raises(T.TLBMError) as e:
+        part.mass()
+    assert e.value.status == T.ERR_NUMERIC

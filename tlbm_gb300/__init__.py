@@ -1,0 +1,304 @@
+"""tlbm_gb300 -- GB300 lattice-Boltzmann engine with the tLBM operator surface.
+
+The engine is ``lib/libtlbm_gb300.so`` (hand-written sm_103a CUDA behind the C ABI of
+``include/tlbm.h``).  This module binds that ABI with ctypes and mirrors the reference's
+``TLBM_Partition`` class (include/TLBM_Partition.h:33-133) for Python callers:
+
+    part = TLBMPartition(workdir)            # TLBM_Partition(rank, size, comm)
+    for ts in range(part.get_num_ts()):
+        part.take_LBM_time_step(ts % 2)      # take_LBM_time_step(bool isEven)
+        if (ts + 1) % part.get_plot_freq() == 0 and ts + 1 > part.get_warmupTs():
+            part.write_data()                # write_data()
+
+Errors raise ``TLBMError`` carrying the C status and message (the reference throws).  There is
+no CPU fallback: if the library is missing, importing the binding fails loudly.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libtlbm_gb300.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "tlbm.h")
+
+# status codes (include/tlbm.h)
+OK, ERR_IO, ERR_INVALID_ARGUMENT, ERR_FORMAT, ERR_OUT_OF_RANGE, ERR_CUDA, ERR_NUMERIC, \
+    ERR_UNSUPPORTED, ERR_TIMEOUT, ERR_NO_MEMORY = range(10)
+PREC = {"f64": 0, "f32": 1, "bf16": 2, "f16": 3}
+ARITH = {"reference": 0, "fast": 1}
+
+
+class TLBMError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__("%s (status %d)" % (message, status))
+        self.status = status
+        self.message = message
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_int), ("precision", ctypes.c_int),
+                ("arithmetic", ctypes.c_int), ("closure", ctypes.c_int),
+                ("block_x", ctypes.c_int), ("block_y", ctypes.c_int), ("device", ctypes.c_int),
+                ("reserved", ctypes.c_int * 9)]
+
+
+class Problem(ctypes.Structure):
+    _fields_ = [("lattice", ctypes.c_char * 8), ("dynamics", ctypes.c_int),
+                ("num_ts", ctypes.c_int), ("ts_rep_freq", ctypes.c_int),
+                ("warmup_ts", ctypes.c_int), ("plot_freq", ctypes.c_int),
+                ("cs", ctypes.c_double), ("rho_lbm", ctypes.c_double),
+                ("u_lbm", ctypes.c_double), ("omega", ctypes.c_double),
+                ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+                ("restart_flag", ctypes.c_int), ("time_avg_flag", ctypes.c_int),
+                ("lx_p", ctypes.c_double), ("ly_p", ctypes.c_double), ("lz_p", ctypes.c_double),
+                ("t_conv", ctypes.c_double), ("l_conv", ctypes.c_double),
+                ("p_conv", ctypes.c_double), ("p_ref_idx", ctypes.c_int),
+                ("ss_data_flag", ctypes.c_int)]
+
+
+_lib = None
+
+
+def library(path: str = LIB_PATH):
+    """Load the engine library (ctypes) and declare its signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError("tlbm_gb300 engine library not built (%s); run "
+                          "`python -m tlbm_gb300.build`" % path)
+    L = ctypes.CDLL(path)
+    vp, i32, i64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64
+    H = ctypes.c_void_p
+    PH = ctypes.POINTER(ctypes.c_void_p)
+    sig = {
+        "tlbm_default_options": (None, [ctypes.POINTER(Options)]),
+        "tlbm_create": (i32, [ctypes.c_char_p, i32, i32, PH]),
+        "tlbm_create_ex": (i32, [ctypes.c_char_p, i32, i32, ctypes.POINTER(Options), PH]),
+        "tlbm_create_from_arrays": (i32, [ctypes.POINTER(Problem), vp, vp, ctypes.c_char_p,
+                                          ctypes.POINTER(Options), PH]),
+        "tlbm_destroy": (i32, [H]),
+        "tlbm_step": (i32, [H, i32]),
+        "tlbm_run": (i32, [H, i32, i32]),
+        "tlbm_time_steps": (i32, [H, i32, i32, ctypes.POINTER(ctypes.c_float)]),
+        "tlbm_synchronize": (i32, [H]),
+        "tlbm_write_data": (i32, [H]),
+        "tlbm_write_time_avg_data": (i32, [H]),
+        "tlbm_get_num_ts": (i32, [H]),
+        "tlbm_get_ts_rep_freq": (i32, [H]),
+        "tlbm_get_plot_freq": (i32, [H]),
+        "tlbm_get_warmup_ts": (i32, [H]),
+        "tlbm_get_num_global_nodes": (i32, [H]),
+        "tlbm_get_time_avg_flag": (i32, [H]),
+        "tlbm_is_restart": (i32, [H]),
+        "tlbm_get_cut_size": (i32, [H]),
+        "tlbm_get_last_error": (ctypes.c_char_p, [H]),
+        "tlbm_status_string": (ctypes.c_char_p, [i32]),
+        "tlbm_output_bytes": (i32, [H]),
+        "tlbm_num_speeds": (i32, [H]),
+        "tlbm_copy_macros": (i32, [H, vp, vp, vp, vp]),
+        "tlbm_copy_force": (i32, [H, vp, vp, vp]),
+        "tlbm_copy_populations": (i32, [H, i32, vp]),
+        "tlbm_copy_adjacency": (i32, [H, vp]),
+        "tlbm_mass": (i32, [H, ctypes.POINTER(ctypes.c_double)]),
+        "tlbm_kernel_launches": (i64, [H]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def declared_symbols(header: str = HEADER) -> list[str]:
+    """Function names declared in include/tlbm.h."""
+    text = open(header).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(tlbm_[a-z_0-9]+)\s*\(", text)))
+
+
+def options(precision="f32", arithmetic=None, block_x=0, block_y=0, device=0) -> Options:
+    o = Options()
+    library().tlbm_default_options(ctypes.byref(o))
+    o.precision = PREC[precision]
+    if arithmetic is None:
+        arithmetic = "fast" if precision in ("bf16", "f16") else "reference"
+    o.arithmetic = ARITH[arithmetic]
+    o.block_x, o.block_y, o.device = block_x, block_y, device
+    return o
+
+
+def _check(status: int, handle=None) -> None:
+    if status != OK:
+        L = library()
+        msg = L.tlbm_get_last_error(handle).decode()
+        raise TLBMError(status, msg or L.tlbm_status_string(status).decode())
+
+
+class TLBMPartition:
+    """The reference's TLBM_Partition over the GPU engine (one process, whole lattice)."""
+
+    def __init__(self, workdir: str = ".", rank: int = 0, size: int = 1 << 20,
+                 precision: str | None = None, arithmetic: str | None = None,
+                 block_x: int = 0, block_y: int = 0, device: int = 0, _handle=None):
+        self._L = library()
+        self._h = ctypes.c_void_p()
+        self.workdir = workdir
+        if _handle is not None:
+            self._h = _handle
+        elif precision is None and arithmetic is None:
+            # like the reference binary: defaults, optionally overridden by workdir/tlbm.cfg
+            _check(self._L.tlbm_create(workdir.encode(), rank, size, ctypes.byref(self._h)))
+        else:
+            o = options(precision or "f32", arithmetic, block_x, block_y, device)
+            _check(self._L.tlbm_create_ex(workdir.encode(), rank, size, ctypes.byref(o),
+                                          ctypes.byref(self._h)))
+        self._init_meta()
+
+    @classmethod
+    def from_arrays(cls, problem: Problem, nd_type, parts=None, workdir=None,
+                    precision="f64", arithmetic=None, block_x=0, block_y=0, device=0):
+        L = library()
+        nd = np.ascontiguousarray(nd_type, dtype=np.int32)
+        pp = None if parts is None else np.ascontiguousarray(parts, dtype=np.int32)
+        o = options(precision, arithmetic, block_x, block_y, device)
+        h = ctypes.c_void_p()
+        _check(L.tlbm_create_from_arrays(ctypes.byref(problem), nd.ctypes.data,
+                                         None if pp is None else pp.ctypes.data,
+                                         None if workdir is None else workdir.encode(),
+                                         ctypes.byref(o), ctypes.byref(h)))
+        obj = cls.__new__(cls)
+        obj._L = L
+        obj._h = h
+        obj.workdir = workdir
+        obj._init_meta()
+        return obj
+
+    def _init_meta(self):
+        self.n = self._L.tlbm_get_num_global_nodes(self._h)
+        self.q = self._L.tlbm_num_speeds(self._h)
+        self.dtype = np.float64 if self._L.tlbm_output_bytes(self._h) == 8 else np.float32
+
+    # -- the reference's public surface ---------------------------------------------------
+    def take_LBM_time_step(self, is_even) -> None:
+        _check(self._L.tlbm_step(self._h, int(bool(is_even))), self._h)
+
+    def write_data(self) -> None:
+        _check(self._L.tlbm_write_data(self._h), self._h)
+
+    def write_time_avg_data(self) -> None:
+        _check(self._L.tlbm_write_time_avg_data(self._h), self._h)
+
+    def get_num_ts(self) -> int:
+        return self._L.tlbm_get_num_ts(self._h)
+
+    def get_ts_rep_freq(self) -> int:
+        return self._L.tlbm_get_ts_rep_freq(self._h)
+
+    def get_plot_freq(self) -> int:
+        return self._L.tlbm_get_plot_freq(self._h)
+
+    def get_warmupTs(self) -> int:
+        return self._L.tlbm_get_warmup_ts(self._h)
+
+    def get_num_global_nodes(self) -> int:
+        return self._L.tlbm_get_num_global_nodes(self._h)
+
+    def get_time_avg_flag(self) -> int:
+        return self._L.tlbm_get_time_avg_flag(self._h)
+
+    def is_restart(self) -> int:
+        return self._L.tlbm_is_restart(self._h)
+
+    def get_cut_size(self) -> int:
+        return self._L.tlbm_get_cut_size(self._h)
+
+    # -- engine extras -----------------------------------------------------------------------
+    def run(self, first_ts: int, nsteps: int) -> None:
+        _check(self._L.tlbm_run(self._h, first_ts, nsteps), self._h)
+
+    def time_steps(self, first_ts: int, nsteps: int) -> float:
+        ms = ctypes.c_float(0.0)
+        _check(self._L.tlbm_time_steps(self._h, first_ts, nsteps, ctypes.byref(ms)), self._h)
+        return ms.value
+
+    def synchronize(self) -> None:
+        _check(self._L.tlbm_synchronize(self._h), self._h)
+
+    def macros(self):
+        out = [np.empty(self.n, self.dtype) for _ in range(4)]
+        _check(self._L.tlbm_copy_macros(self._h, *[a.ctypes.data for a in out]), self._h)
+        return out
+
+    def force(self):
+        out = [np.empty(self.n, self.dtype) for _ in range(3)]
+        _check(self._L.tlbm_copy_force(self._h, *[a.ctypes.data for a in out]), self._h)
+        return out
+
+    def populations(self, which: int = 0):
+        out = np.empty(self.n * self.q, self.dtype)
+        _check(self._L.tlbm_copy_populations(self._h, which, out.ctypes.data), self._h)
+        return out
+
+    def adjacency(self):
+        out = np.empty(self.n * self.q, np.int32)
+        _check(self._L.tlbm_copy_adjacency(self._h, out.ctypes.data), self._h)
+        return out
+
+    def mass(self) -> float:
+        m = ctypes.c_double(0.0)
+        _check(self._L.tlbm_mass(self._h, ctypes.byref(m)), self._h)
+        return m.value
+
+    def kernel_launches(self) -> int:
+        return self._L.tlbm_kernel_launches(self._h)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.tlbm_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def problem_from_params(p) -> Problem:
+    """ctypes Problem from a ``geometry.Params``."""
+    pr = Problem()
+    pr.lattice = p.lattice.encode()
+    for f in ("dynamics", "num_ts", "ts_rep_freq", "warmup_ts", "plot_freq", "nx", "ny", "nz",
+              "p_ref_idx"):
+        setattr(pr, f, int(getattr(p, f)))
+    pr.restart_flag = int(p.restart)
+    pr.time_avg_flag = int(p.time_avg)
+    pr.ss_data_flag = int(p.ss_flag)
+    for f in ("cs", "rho_lbm", "u_lbm", "omega", "lx_p", "ly_p", "lz_p"):
+        setattr(pr, f, float(getattr(p, f)))
+    pr.t_conv, pr.l_conv, pr.p_conv = float(p.t_conv), float(p.l_conv), float(p.p_conv)
+    return pr
+
+
+def run_like_tlbmexec(part: TLBMPartition) -> None:
+    """The reference's main loop (src/tLBM.cpp:45-61) over a partition."""
+    nts, pf, wu = part.get_num_ts(), part.get_plot_freq(), part.get_warmupTs()
+    for ts in range(nts):
+        part.take_LBM_time_step(ts % 2)
+        if (ts + 1) % pf == 0 and ts + 1 > wu:
+            part.write_data()
+    if part.get_time_avg_flag() == 1:
+        part.write_time_avg_data()

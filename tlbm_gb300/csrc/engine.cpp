@@ -1,0 +1,664 @@
+// engine.cpp -- host side of the engine: inputs, device memory, step launches, dumps.
+//
+// It restates TLBM_Partition's initialisation and output pipeline (src/TLBM_Partition.cpp)
+// for a lattice that lives whole on one GPU:
+//   * load_input / load_ndType / load_parts      -> parse_* below (same files, same order)
+//   * create_adj_matrix / compute_halo_data       -> no tables: neighbours are computed in the
+//     kernels; the halo exchange vanishes (one global array); get_cut_size is still reported
+//   * allocate_arrays / initialize_data_arrays    -> two SoA population buffers on the device
+//   * write_node_ordering / write_data            -> partition-major order (writeOffset), the
+//     same file names and raw layout, MPI_File_write_at semantics (create, no truncation)
+#include "engine.h"
+
+#include <fcntl.h>
+#include <unistd.h>
+
+#include <algorithm>
+#include <cerrno>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+
+namespace tlbm {
+
+// ----------------------------------------------------------------------------- input parsing
+
+Status read_text(const std::string& path, std::string* out) {
+  std::ifstream in(path, std::ios::in | std::ios::binary);
+  if (!in.is_open()) return Status::err(TLBM_ERR_IO, "Could not open " + path + "!");
+  std::ostringstream ss;
+  ss << in.rdbuf();
+  *out = ss.str();
+  return Status::ok();
+}
+
+namespace {
+
+template <class T>
+bool parse_token(const std::string& tok, T* v) {
+  std::istringstream is(tok);
+  T x;
+  is >> x;
+  if (is.fail()) return false;
+  // accept the token only if it was consumed entirely
+  char rest;
+  if (is >> rest) return false;
+  *v = x;
+  return true;
+}
+
+bool parse_real(const std::string& tok, bool as_float, double* v) {
+  if (as_float) {
+    float f;
+    if (!parse_token(tok, &f)) return false;
+    *v = static_cast<double>(f);
+    return true;
+  }
+  return parse_token(tok, v);
+}
+
+}  // namespace
+
+Status parse_params(const std::string& text, bool as_float, tlbm_problem* p) {
+  std::istringstream is(text);
+  std::vector<std::string> tok;
+  std::string t;
+  while (tok.size() < 23 && (is >> t)) tok.push_back(t);
+  // the solver needs the first 15 tokens; the rest only feed post-processing
+  if (tok.size() < 15)
+    return Status::err(TLBM_ERR_FORMAT, "params.lbm has " + std::to_string(tok.size()) +
+                                            " values; at least 15 are required");
+  std::memset(p, 0, sizeof(*p));
+  if (tok[0].size() >= sizeof(p->lattice))
+    return Status::err(TLBM_ERR_INVALID_ARGUMENT, "Invalid Lattice Structure!");
+  std::snprintf(p->lattice, sizeof(p->lattice), "%s", tok[0].c_str());
+  bool ok = true;
+  int* ints[] = {&p->dynamics, &p->num_ts, &p->ts_rep_freq, &p->warmup_ts, &p->plot_freq};
+  for (int k = 0; k < 5; ++k) ok = ok && parse_token(tok[1 + k], ints[k]);
+  double* reals[] = {&p->cs, &p->rho_lbm, &p->u_lbm, &p->omega};
+  for (int k = 0; k < 4; ++k) ok = ok && parse_real(tok[6 + k], as_float, reals[k]);
+  int* dims[] = {&p->nx, &p->ny, &p->nz, &p->restart_flag, &p->time_avg_flag};
+  for (int k = 0; k < 5; ++k) ok = ok && parse_token(tok[10 + k], dims[k]);
+  if (!ok) return Status::err(TLBM_ERR_FORMAT, "params.lbm: malformed value in lines 2-15");
+  double* phys[] = {&p->lx_p, &p->ly_p, &p->lz_p, &p->t_conv, &p->l_conv, &p->p_conv};
+  for (int k = 0; k < 6 && 15 + k < (int)tok.size(); ++k)
+    if (!parse_real(tok[15 + k], as_float, phys[k]))
+      return Status::err(TLBM_ERR_FORMAT, "params.lbm: malformed value on line " +
+                                              std::to_string(16 + k));
+  if (tok.size() > 21 && !parse_token(tok[21], &p->p_ref_idx))
+    return Status::err(TLBM_ERR_FORMAT, "params.lbm: malformed pRefIdx");
+  if (tok.size() > 22 && !parse_token(tok[22], &p->ss_data_flag))
+    return Status::err(TLBM_ERR_FORMAT, "params.lbm: malformed ssDataFlag");
+  return Status::ok();
+}
+
+Status parse_int_file(const std::string& path, int64_t n, std::vector<int32_t>* out) {
+  std::string text;
+  Status s = read_text(path, &text);
+  if (!s.good()) return s;
+  out->assign(static_cast<size_t>(n), 0);
+  const char* c = text.data();
+  const char* end = c + text.size();
+  int64_t k = 0;
+  while (true) {
+    while (c < end && (*c == ' ' || *c == '\n' || *c == '\t' || *c == '\r')) ++c;
+    if (c >= end) break;
+    bool neg = false;
+    if (*c == '-' || *c == '+') {
+      neg = (*c == '-');
+      ++c;
+    }
+    if (c >= end || *c < '0' || *c > '9')
+      return Status::err(TLBM_ERR_FORMAT, path + ": non-integer value at entry " +
+                                              std::to_string(k));
+    int64_t v = 0;
+    while (c < end && *c >= '0' && *c <= '9') {
+      v = v * 10 + (*c - '0');
+      if (v > 2147483647LL) return Status::err(TLBM_ERR_FORMAT, path + ": value out of range");
+      ++c;
+    }
+    if (c < end && !(*c == ' ' || *c == '\n' || *c == '\t' || *c == '\r'))
+      return Status::err(TLBM_ERR_FORMAT, path + ": non-integer value at entry " +
+                                              std::to_string(k));
+    if (k >= n)
+      return Status::err(TLBM_ERR_FORMAT, path + " has more than nx*ny*nz = " +
+                                              std::to_string(n) + " values");
+    (*out)[k++] = static_cast<int32_t>(neg ? -v : v);
+  }
+  if (k != n)
+    return Status::err(TLBM_ERR_FORMAT, path + " has " + std::to_string(k) +
+                                            " values, expected nx*ny*nz = " + std::to_string(n));
+  return Status::ok();
+}
+
+Status apply_config_file(const std::string& path, tlbm_options* opt) {
+  std::ifstream in(path);
+  if (!in.is_open()) return Status::ok();  // optional
+  std::string key, val;
+  while (in >> key >> val) {
+    if (key == "precision") {
+      if (val == "f64") opt->precision = TLBM_PREC_F64;
+      else if (val == "f32") opt->precision = TLBM_PREC_F32;
+      else if (val == "bf16") opt->precision = TLBM_PREC_BF16;
+      else if (val == "f16") opt->precision = TLBM_PREC_F16;
+      else return Status::err(TLBM_ERR_INVALID_ARGUMENT, path + ": unknown precision " + val);
+    } else if (key == "arithmetic") {
+      if (val == "reference") opt->arithmetic = TLBM_ARITH_REFERENCE;
+      else if (val == "fast") opt->arithmetic = TLBM_ARITH_FAST;
+      else return Status::err(TLBM_ERR_INVALID_ARGUMENT, path + ": unknown arithmetic " + val);
+    } else if (key == "block_x") {
+      opt->block_x = std::atoi(val.c_str());
+    } else if (key == "block_y") {
+      opt->block_y = std::atoi(val.c_str());
+    } else if (key == "device") {
+      opt->device = std::atoi(val.c_str());
+    } else {
+      return Status::err(TLBM_ERR_INVALID_ARGUMENT, path + ": unknown key " + key);
+    }
+  }
+  return Status::ok();
+}
+
+// ----------------------------------------------------------------------------- engine
+
+namespace {
+
+int lattice_q(const char* s) {
+  if (!std::strcmp(s, "D3Q15")) return 15;
+  if (!std::strcmp(s, "D3Q19")) return 19;
+  if (!std::strcmp(s, "D3Q27")) return 27;
+  return 0;
+}
+
+// MPI_File_write_at with MPI_MODE_CREATE|MPI_MODE_WRONLY: create, keep existing bytes
+Status write_at(const std::string& path, const void* buf, size_t bytes, size_t offset) {
+  int fd = ::open(path.c_str(), O_WRONLY | O_CREAT, 0644);
+  if (fd < 0) return Status::err(TLBM_ERR_IO, "Error opening file to write " + path);
+  const char* p = static_cast<const char*>(buf);
+  size_t done = 0;
+  while (done < bytes) {
+    ssize_t w = ::pwrite(fd, p + done, bytes - done, static_cast<off_t>(offset + done));
+    if (w < 0) {
+      if (errno == EINTR) continue;
+      ::close(fd);
+      return Status::err(TLBM_ERR_IO, "Error writing " + path);
+    }
+    done += static_cast<size_t>(w);
+  }
+  ::close(fd);
+  return Status::ok();
+}
+
+}  // namespace
+
+Status Engine::check(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return Status::ok();
+  return Status::err(TLBM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define TLBM_TRY(expr)                 \
+  do {                                 \
+    Status _s = (expr);                \
+    if (!_s.good()) return _s;         \
+  } while (0)
+#define TLBM_CUDA(expr) TLBM_TRY(check((expr), #expr))
+
+Engine::~Engine() {
+  if (stream_) cudaStreamSynchronize(stream_);
+  for (auto& g : graph_)
+    if (g) cudaGraphExecDestroy(g);
+  cudaFree(d_type_);
+  for (auto p : d_f_) cudaFree(p);
+  for (auto p : d_macro_) cudaFree(p);
+  for (auto p : d_force_) cudaFree(p);
+  for (auto p : d_avg_) cudaFree(p);
+  for (auto p : d_uyq_) cudaFree(p);
+  cudaFree(d_stage_);
+  cudaFree(d_order_);
+  cudaFree(d_partial_);
+  cudaFree(d_mass_);
+  if (h_pinned_) cudaFreeHost(h_pinned_);
+  if (stream_) cudaStreamDestroy(stream_);
+}
+
+Status Engine::create(const tlbm_problem& prob, const int32_t* nd_type, const int32_t* parts,
+                      int size, const std::string& workdir, const tlbm_options& opt,
+                      Engine** out) {
+  *out = nullptr;
+  Engine* e = new (std::nothrow) Engine();
+  if (!e) return Status::err(TLBM_ERR_NO_MEMORY, "out of host memory");
+  e->prob_ = prob;
+  e->opt_ = opt;
+  e->workdir_ = workdir;
+  Status s = e->init(nd_type, parts, size);
+  if (!s.good()) {
+    delete e;
+    return s;
+  }
+  *out = e;
+  return Status::ok();
+}
+
+Status Engine::init(const int32_t* nd_type, const int32_t* parts, int size) {
+  q_ = lattice_q(prob_.lattice);
+  if (!q_) return Status::err(TLBM_ERR_INVALID_ARGUMENT, "Invalid Lattice Structure!");
+  if (prob_.nx < 1 || prob_.ny < 1 || prob_.nz < 1)
+    return Status::err(TLBM_ERR_FORMAT, "params.lbm: lattice dimensions must be positive");
+  n_ = static_cast<int64_t>(prob_.nx) * prob_.ny * prob_.nz;
+  if (n_ * q_ > (int64_t(1) << 40) || n_ >= (int64_t(1) << 31))
+    return Status::err(TLBM_ERR_UNSUPPORTED, "lattice too large for one device (N >= 2^31)");
+  if (prob_.nz > 65535 || prob_.ny > 65535 * 64)
+    return Status::err(TLBM_ERR_UNSUPPORTED, "nz > 65535 is not supported");
+  if (prob_.plot_freq <= 0)
+    return Status::err(TLBM_ERR_FORMAT, "params.lbm: plotFreq must be positive");
+  switch (opt_.precision) {
+    case TLBM_PREC_F64: store_ = kStoreF64; break;
+    case TLBM_PREC_F32: store_ = kStoreF32; break;
+    case TLBM_PREC_BF16: store_ = kStoreBF16; break;
+    case TLBM_PREC_F16: store_ = kStoreF16; break;
+    default: return Status::err(TLBM_ERR_INVALID_ARGUMENT, "unknown precision option");
+  }
+  ref_arith_ = (opt_.arithmetic == TLBM_ARITH_REFERENCE);
+  if (ref_arith_ && (store_ == kStoreBF16 || store_ == kStoreF16))
+    return Status::err(TLBM_ERR_INVALID_ARGUMENT,
+                       "16-bit storage has no reference arithmetic; use TLBM_ARITH_FAST");
+  if (opt_.closure != TLBM_CLOSURE_PARAMS)
+    return Status::err(TLBM_ERR_UNSUPPORTED, "closure option not available");
+  sb_ = store_bytes(store_);
+  ob_ = (store_ == kStoreF64) ? 8 : 4;
+
+  // node types: the reference's codes only (python/FluidChannel.py:1386-1397)
+  std::vector<uint8_t> types(static_cast<size_t>(n_));
+  for (int64_t g = 0; g < n_; ++g) {
+    const int32_t t = nd_type[g];
+    if (!(t == 0 || t == 1 || t == 2 || t == 3 || t == 5))
+      return Status::err(TLBM_ERR_OUT_OF_RANGE, "ndType.lbm: node " + std::to_string(g) +
+                                                    " has unknown type " + std::to_string(t));
+    types[g] = static_cast<uint8_t>(t);
+    if (t == 5) has_type5_ = true;
+  }
+
+  // partitions: the reference indexes partSizes[p] with p < size (src/TLBM_Partition.cpp:224)
+  if (size < 1) return Status::err(TLBM_ERR_INVALID_ARGUMENT, "size must be >= 1");
+  int32_t max_part = 0;
+  identity_order_ = true;
+  if (parts) {
+    for (int64_t g = 0; g < n_; ++g) {
+      const int32_t p = parts[g];
+      if (p < 0 || p >= size)
+        return Status::err(TLBM_ERR_OUT_OF_RANGE,
+                           "parts.lbm: node " + std::to_string(g) + " is in partition " +
+                               std::to_string(p) + " but the job size is " +
+                               std::to_string(size));
+      max_part = std::max(max_part, p);
+      if (g > 0 && p < parts[g - 1]) identity_order_ = false;
+    }
+  }
+  if (parts && !identity_order_) {
+    // nodes sorted by (partition, global id): the concatenation of every rank's localNdList
+    // written at its writeOffset (src/TLBM_Partition.cpp:244-248, :542-561)
+    std::vector<int64_t> count(static_cast<size_t>(max_part) + 2, 0);
+    for (int64_t g = 0; g < n_; ++g) count[parts[g] + 1]++;
+    for (int p = 0; p <= max_part; ++p) count[p + 1] += count[p];
+    order_.assign(static_cast<size_t>(n_), 0);
+    for (int64_t g = 0; g < n_; ++g) order_[count[parts[g]]++] = static_cast<int32_t>(g);
+  }
+  // cut size of partition 0: (node, speed) pairs of rank 0 whose push target lies elsewhere
+  cut_size_ = 0;
+  if (parts) {
+    bool multi = false;
+    for (int64_t g = 0; g < n_ && !multi; ++g) multi = parts[g] != parts[0];
+    if (multi) {
+      const int nx = prob_.nx, ny = prob_.ny, nz = prob_.nz;
+      const int64_t nxy = static_cast<int64_t>(nx) * ny;
+      auto tables = [&](int q, const int** ex, const int** ey, const int** ez) {
+        static const int e15x[] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1};
+        static const int e15y[] = {0, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1};
+        static const int e15z[] = {0, 0, 0, 0, 0, 1, -1, 1, 1, 1, 1, -1, -1, -1, -1};
+        static int e19x[19], e19y[19], e19z[19], e27x[27], e27y[27], e27z[27];
+        for (int i = 0; i < 19; ++i) {
+          e19x[i] = Lattice<19>::ex(i); e19y[i] = Lattice<19>::ey(i); e19z[i] = Lattice<19>::ez(i);
+        }
+        for (int i = 0; i < 27; ++i) {
+          e27x[i] = Lattice<27>::ex(i); e27y[i] = Lattice<27>::ey(i); e27z[i] = Lattice<27>::ez(i);
+        }
+        if (q == 15) { *ex = e15x; *ey = e15y; *ez = e15z; }
+        else if (q == 19) { *ex = e19x; *ey = e19y; *ez = e19z; }
+        else { *ex = e27x; *ey = e27y; *ez = e27z; }
+      };
+      const int *ex, *ey, *ez;
+      tables(q_, &ex, &ey, &ez);
+      for (int64_t g = 0; g < n_; ++g) {
+        if (parts[g] != 0) continue;
+        const int z = static_cast<int>(g / nxy);
+        const int y = static_cast<int>((g - z * nxy) / nx);
+        const int x = static_cast<int>(g - z * nxy - static_cast<int64_t>(y) * nx);
+        for (int i = 0; i < q_; ++i) {
+          const int tx = ((x + ex[i]) % nx + nx) % nx, ty = ((y + ey[i]) % ny + ny) % ny,
+                    tz = ((z + ez[i]) % nz + nz) % nz;
+          const int64_t tg = tx + static_cast<int64_t>(ty) * nx + tz * nxy;
+          if (parts[tg] != 0) cut_size_++;
+        }
+      }
+    }
+  }
+
+  TLBM_CUDA(cudaSetDevice(opt_.device));
+  TLBM_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  launch_.stream = stream_;
+  int bx = opt_.block_x, by = opt_.block_y;
+  if (bx <= 0) bx = prob_.nx >= 128 ? 128 : 32;
+  if (by <= 0) by = std::max(1, 128 / bx);
+  if (bx * by > 128 || bx % 32 != 0)
+    return Status::err(TLBM_ERR_INVALID_ARGUMENT,
+                       "block_x must be a multiple of 32 and block_x*block_y <= 128");
+  launch_.bx = bx;
+  launch_.by = by;
+
+  const size_t n = static_cast<size_t>(n_);
+  TLBM_CUDA(cudaMalloc(&d_type_, n));
+  TLBM_CUDA(cudaMemcpy(d_type_, types.data(), n, cudaMemcpyHostToDevice));
+  for (auto& p : d_f_) TLBM_CUDA(cudaMalloc(&p, n * q_ * sb_));
+  for (auto& p : d_macro_) TLBM_CUDA(cudaMalloc(&p, n * ob_));
+  for (auto& p : d_force_) TLBM_CUDA(cudaMalloc(&p, n * ob_));
+  if (prob_.time_avg_flag == 1) {
+    for (auto& p : d_avg_) {
+      TLBM_CUDA(cudaMalloc(&p, n * ob_));
+      TLBM_CUDA(cudaMemsetAsync(p, 0, n * ob_, stream_));
+    }
+  }
+  for (auto& p : d_uyq_) {
+    TLBM_CUDA(cudaMalloc(&p, 32 * 8));
+    TLBM_CUDA(cudaMemsetAsync(p, 0, 32 * 8, stream_));
+  }
+  if (!identity_order_) {
+    TLBM_CUDA(cudaMalloc(&d_order_, n * sizeof(int32_t)));
+    TLBM_CUDA(cudaMemcpy(d_order_, order_.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice));
+    TLBM_CUDA(cudaMalloc(&d_stage_, n * ob_));
+  }
+
+  pb_.nx = prob_.nx;
+  pb_.ny = prob_.ny;
+  pb_.nz = prob_.nz;
+  pb_.nxy = prob_.nx * prob_.ny;
+  pb_.n = n_;
+  pb_.nd_type = d_type_;
+  pb_.omega = prob_.omega;
+  pb_.cs = prob_.cs;
+  pb_.u_bc = prob_.u_lbm;
+  pb_.rho_bc = prob_.rho_lbm;
+  pb_.dynamics = prob_.dynamics;
+  pb_.has_type5 = has_type5_ ? 1 : 0;
+
+  const int nb = mass_blocks(pb_);
+  TLBM_CUDA(cudaMalloc(&d_partial_, nb * sizeof(double)));
+  TLBM_CUDA(cudaMalloc(&d_mass_, sizeof(double)));
+
+  if (prob_.restart_flag)
+    return Status::err(TLBM_ERR_UNSUPPORTED,
+                       "restart (params.lbm line 14) needs restart data; not available here");
+  // f = w*rho in both buffers (initialize_data_arrays, src/TLBM_Partition.cpp:458-465)
+  for (auto p : d_f_) {
+    TLBM_CUDA(launch_init_uniform(q_, store_, pb_, p, prob_.rho_lbm, launch_));
+    ++launches_;
+  }
+  TLBM_CUDA(cudaStreamSynchronize(stream_));
+  TLBM_CUDA(cudaMallocHost(&h_pinned_, n * std::max(ob_, 4)));
+
+  // write_node_ordering (src/TLBM_Partition.cpp:542-561)
+  if (!workdir_.empty()) {
+    std::vector<int32_t> ord;
+    const int32_t* op = order_.data();
+    if (identity_order_) {
+      ord.resize(n);
+      for (size_t g = 0; g < n; ++g) ord[g] = static_cast<int32_t>(g);
+      op = ord.data();
+    }
+    TLBM_TRY(write_at(workdir_ + "/ordering.b_dat", op, n * sizeof(int32_t), 0));
+  }
+  return Status::ok();
+}
+
+Status Engine::enqueue_step(int is_even) {
+  // take_LBM_time_step: isEven -> fIn = fEven, fOut = fOdd (src/TLBM_Partition.cpp:913-920).
+  // Here the pull reads the buffer the reference calls fIn and writes the other one.
+  const int src = is_even ? 0 : 1;
+  const int dst = 1 - src;
+  StepArgs a{};
+  a.pb = pb_;
+  a.src = d_f_[src];
+  a.dst = d_f_[dst];
+  a.time_avg = (prob_.time_avg_flag == 1) ? 1 : 0;
+  for (int k = 0; k < 4; ++k) a.avg[k] = d_avg_[k];
+  const int par = is_even ? 1 : 0;
+  a.uyq_cur = d_uyq_[par];
+  a.uyq_prev = d_uyq_[1 - par];
+  if (ref_arith_) {
+    if (has_type5_) {
+      TLBM_CUDA(launch_quirk_uy_ref(q_, sb_, pb_, a.src, d_uyq_[par], launch_));
+      ++launches_;
+    }
+    TLBM_CUDA(launch_step_ref(q_, sb_, a, launch_));
+  } else {
+    TLBM_CUDA(launch_step_fast(q_, store_, a, launch_));
+    if (has_type5_) ++launches_;
+  }
+  ++launches_;
+  last_src_ = src;
+  last_dst_ = dst;
+  outputs_fresh_ = false;
+  ++steps_;
+  return Status::ok();
+}
+
+Status Engine::step(int is_even) {
+  TLBM_CUDA(cudaSetDevice(opt_.device));
+  return enqueue_step(is_even);
+}
+
+Status Engine::build_graph(int parity) {
+  // two consecutive steps starting with is_even = parity, captured once
+  if (graph_[parity]) return Status::ok();
+  cudaGraph_t g = nullptr;
+  TLBM_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+  const int64_t l0 = launches_;
+  Status s = enqueue_step(parity);
+  if (s.good()) s = enqueue_step(1 - parity);
+  cudaError_t e = cudaStreamEndCapture(stream_, &g);
+  launches_ = l0;
+  steps_ -= 2;
+  if (!s.good()) {
+    if (g) cudaGraphDestroy(g);
+    return s;
+  }
+  TLBM_CUDA(e);
+  e = cudaGraphInstantiate(&graph_[parity], g, 0);
+  cudaGraphDestroy(g);
+  TLBM_CUDA(e);
+  return Status::ok();
+}
+
+Status Engine::run(int first_ts, int nsteps) {
+  TLBM_CUDA(cudaSetDevice(opt_.device));
+  if (nsteps < 0) return Status::err(TLBM_ERR_INVALID_ARGUMENT, "nsteps < 0");
+  int ts = first_ts;
+  const int64_t per_step = has_type5_ ? 2 : 1;
+  if (nsteps >= 2) {
+    const int parity = ts % 2;
+    TLBM_TRY(build_graph(parity));
+    while (nsteps >= 2) {
+      TLBM_CUDA(cudaGraphLaunch(graph_[parity], stream_));
+      launches_ += 2 * per_step;
+      steps_ += 2;
+      ts += 2;
+      nsteps -= 2;
+    }
+    // the last captured step had is_even = 1 - parity, i.e. it pulled from buffer `parity`
+    last_src_ = parity;
+    last_dst_ = 1 - parity;
+    outputs_fresh_ = false;
+  }
+  if (nsteps == 1) TLBM_TRY(enqueue_step(ts % 2));
+  return Status::ok();
+}
+
+Status Engine::time_steps(int first_ts, int nsteps, float* ms) {
+  TLBM_CUDA(cudaSetDevice(opt_.device));
+  cudaEvent_t e0, e1;
+  TLBM_CUDA(cudaEventCreate(&e0));
+  TLBM_CUDA(cudaEventCreate(&e1));
+  TLBM_CUDA(cudaStreamSynchronize(stream_));
+  TLBM_CUDA(cudaEventRecord(e0, stream_));
+  Status s = run(first_ts, nsteps);
+  if (s.good()) s = check(cudaEventRecord(e1, stream_), "cudaEventRecord");
+  if (s.good()) s = check(cudaEventSynchronize(e1), "step loop");
+  if (s.good()) s = check(cudaEventElapsedTime(ms, e0, e1), "cudaEventElapsedTime");
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return s;
+}
+
+Status Engine::synchronize() {
+  TLBM_CUDA(cudaSetDevice(opt_.device));
+  TLBM_CUDA(cudaStreamSynchronize(stream_));
+  return Status::ok();
+}
+
+Status Engine::compute_outputs() {
+  if (last_src_ < 0)
+    return Status::err(TLBM_ERR_INVALID_ARGUMENT, "no time step has been taken yet");
+  if (outputs_fresh_) return Status::ok();
+  // macroscopic values of the last step, recomputed from its (untouched) pull source
+  if (ref_arith_) {
+    TLBM_CUDA(launch_macros_ref(q_, sb_, pb_, d_f_[last_src_], d_macro_, launch_));
+    TLBM_CUDA(launch_force_ref(q_, sb_, pb_, d_f_[last_dst_], d_force_, launch_));
+  } else {
+    TLBM_CUDA(launch_macros_fast(q_, store_, pb_, d_f_[last_src_], d_macro_, launch_));
+    TLBM_CUDA(launch_force_fast(q_, store_, pb_, d_f_[last_dst_], d_force_, launch_));
+  }
+  launches_ += 2;
+  outputs_fresh_ = true;
+  return Status::ok();
+}
+
+Status Engine::fetch(const void* dev, void* host) {
+  const size_t bytes = static_cast<size_t>(n_) * ob_;
+  const void* from = dev;
+  if (!identity_order_) {
+    TLBM_CUDA(launch_gather(dev, d_order_, n_, ob_, d_stage_, launch_));
+    ++launches_;
+    from = d_stage_;
+  }
+  TLBM_CUDA(cudaMemcpyAsync(host, from, bytes, cudaMemcpyDeviceToHost, stream_));
+  TLBM_CUDA(cudaStreamSynchronize(stream_));
+  return Status::ok();
+}
+
+Status Engine::write_field(const std::string& name, const void* dev) {
+  TLBM_TRY(fetch(dev, h_pinned_));
+  return write_at(workdir_ + "/" + name, h_pinned_, static_cast<size_t>(n_) * ob_, 0);
+}
+
+Status Engine::write_data() {
+  TLBM_CUDA(cudaSetDevice(opt_.device));
+  if (workdir_.empty()) return Status::err(TLBM_ERR_IO, "no output directory");
+  TLBM_TRY(compute_outputs());
+  const std::string d = std::to_string(dump_num_);
+  TLBM_TRY(write_field("ux" + d + ".b_dat", d_macro_[0]));
+  TLBM_TRY(write_field("uy" + d + ".b_dat", d_macro_[1]));
+  TLBM_TRY(write_field("uz" + d + ".b_dat", d_macro_[2]));
+  TLBM_TRY(write_field("density" + d + ".b_dat", d_macro_[3]));
+  TLBM_TRY(write_field("Fx" + d + ".b_dat", d_force_[0]));
+  TLBM_TRY(write_field("Fy" + d + ".b_dat", d_force_[1]));
+  TLBM_TRY(write_field("Fz" + d + ".b_dat", d_force_[2]));
+  ++dump_num_;
+  return Status::ok();
+}
+
+Status Engine::write_time_avg_data() {
+  TLBM_CUDA(cudaSetDevice(opt_.device));
+  if (prob_.time_avg_flag != 1)
+    return Status::err(TLBM_ERR_INVALID_ARGUMENT, "time averaging is off (params.lbm line 15)");
+  if (workdir_.empty()) return Status::err(TLBM_ERR_IO, "no output directory");
+  TLBM_TRY(write_field("uAvg.b_dat", d_avg_[0]));
+  TLBM_TRY(write_field("vAvg.b_dat", d_avg_[1]));
+  TLBM_TRY(write_field("wAvg.b_dat", d_avg_[2]));
+  TLBM_TRY(write_field("rhoAvg.b_dat", d_avg_[3]));
+  return Status::ok();
+}
+
+Status Engine::copy_macros(void* ux, void* uy, void* uz, void* rho) {
+  TLBM_CUDA(cudaSetDevice(opt_.device));
+  TLBM_TRY(compute_outputs());
+  void* o[4] = {ux, uy, uz, rho};
+  const size_t bytes = static_cast<size_t>(n_) * ob_;
+  for (int k = 0; k < 4; ++k) {
+    if (!o[k]) continue;
+    TLBM_CUDA(cudaMemcpyAsync(o[k], d_macro_[k], bytes, cudaMemcpyDeviceToHost, stream_));
+  }
+  TLBM_CUDA(cudaStreamSynchronize(stream_));
+  return Status::ok();
+}
+
+Status Engine::copy_force(void* fx, void* fy, void* fz) {
+  TLBM_CUDA(cudaSetDevice(opt_.device));
+  TLBM_TRY(compute_outputs());
+  void* o[3] = {fx, fy, fz};
+  const size_t bytes = static_cast<size_t>(n_) * ob_;
+  for (int k = 0; k < 3; ++k) {
+    if (!o[k]) continue;
+    TLBM_CUDA(cudaMemcpyAsync(o[k], d_force_[k], bytes, cudaMemcpyDeviceToHost, stream_));
+  }
+  TLBM_CUDA(cudaStreamSynchronize(stream_));
+  return Status::ok();
+}
+
+Status Engine::copy_populations(int which, void* out) {
+  TLBM_CUDA(cudaSetDevice(opt_.device));
+  if (last_src_ < 0) return Status::err(TLBM_ERR_INVALID_ARGUMENT, "no time step taken yet");
+  const size_t bytes = static_cast<size_t>(n_) * q_ * ob_;
+  void* d = nullptr;
+  TLBM_CUDA(cudaMallocAsync(&d, bytes, stream_));
+  // which = 0: post-stream fOut = pull of the last destination; 1: post-collision values
+  cudaError_t e = launch_to_aos(q_, store_, pb_, d_f_[last_dst_], which == 0 ? 1 : 0, d, ob_,
+                                launch_);
+  ++launches_;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, bytes, cudaMemcpyDeviceToHost, stream_);
+  cudaFreeAsync(d, stream_);
+  TLBM_CUDA(e);
+  TLBM_CUDA(cudaStreamSynchronize(stream_));
+  return Status::ok();
+}
+
+Status Engine::copy_adjacency(int32_t* out) {
+  TLBM_CUDA(cudaSetDevice(opt_.device));
+  const size_t bytes = static_cast<size_t>(n_) * q_ * sizeof(int32_t);
+  void* d = nullptr;
+  TLBM_CUDA(cudaMallocAsync(&d, bytes, stream_));
+  cudaError_t e = launch_adjacency(q_, pb_, static_cast<int32_t*>(d), launch_);
+  ++launches_;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, bytes, cudaMemcpyDeviceToHost, stream_);
+  cudaFreeAsync(d, stream_);
+  TLBM_CUDA(e);
+  TLBM_CUDA(cudaStreamSynchronize(stream_));
+  return Status::ok();
+}
+
+Status Engine::mass(double* out) {
+  TLBM_CUDA(cudaSetDevice(opt_.device));
+  // the populations the next step will pull (after a step: its destination)
+  const int buf = last_dst_ >= 0 ? last_dst_ : 1;
+  TLBM_CUDA(launch_mass(q_, store_, pb_, d_f_[buf], d_partial_, mass_blocks(pb_), d_mass_,
+                        launch_));
+  launches_ += 2;
+  TLBM_CUDA(cudaMemcpyAsync(out, d_mass_, sizeof(double), cudaMemcpyDeviceToHost, stream_));
+  TLBM_CUDA(cudaStreamSynchronize(stream_));
+  if (!std::isfinite(*out))
+    return Status::err(TLBM_ERR_NUMERIC, "total mass is not finite: the run has diverged");
+  return Status::ok();
+}
+
+}  // namespace tlbm

@@ -1,0 +1,109 @@
+// engine.h -- the object behind a tlbm_handle: one lattice on one GPU.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/tlbm.h"
+#include "kernels.h"
+
+namespace tlbm {
+
+struct Status {
+  tlbm_status code = TLBM_OK;
+  std::string msg;
+  static Status ok() { return Status(); }
+  static Status err(tlbm_status c, std::string m) {
+    Status s;
+    s.code = c;
+    s.msg = std::move(m);
+    return s;
+  }
+  bool good() const { return code == TLBM_OK; }
+};
+
+// Problem::load_input semantics (src/Problem.cpp:5-32): 23 whitespace-separated tokens.
+// Real values are parsed in the precision that will compute with them.
+Status parse_params(const std::string& text, bool as_float, tlbm_problem* p);
+// whitespace-separated integers of ndType.lbm / parts.lbm, exactly n of them
+Status parse_int_file(const std::string& path, int64_t n, std::vector<int32_t>* out);
+Status read_text(const std::string& path, std::string* out);
+Status apply_config_file(const std::string& path, tlbm_options* opt);
+
+class Engine {
+ public:
+  ~Engine();
+  static Status create(const tlbm_problem& prob, const int32_t* nd_type, const int32_t* parts,
+                       int size, const std::string& workdir, const tlbm_options& opt,
+                       Engine** out);
+
+  Status step(int is_even);
+  Status run(int first_ts, int nsteps);
+  Status time_steps(int first_ts, int nsteps, float* ms);
+  Status synchronize();
+  Status write_data();
+  Status write_time_avg_data();
+  Status copy_macros(void* ux, void* uy, void* uz, void* rho);
+  Status copy_force(void* fx, void* fy, void* fz);
+  Status copy_populations(int which, void* out);
+  Status copy_adjacency(int32_t* out);
+  Status mass(double* out);
+
+  const tlbm_problem& problem() const { return prob_; }
+  int output_bytes() const { return ob_; }
+  int q() const { return q_; }
+  int cut_size() const { return cut_size_; }
+  int64_t launches() const { return launches_; }
+  std::string last_error;
+
+ private:
+  Engine() = default;
+  Status init(const int32_t* nd_type, const int32_t* parts, int size);
+  Status check(cudaError_t e, const char* what);
+  Status enqueue_step(int is_even);
+  Status compute_outputs();
+  Status fetch(const void* dev, void* host);  // one field, global order
+  Status write_field(const std::string& name, const void* dev);
+  Status build_graph(int parity);
+
+  tlbm_problem prob_{};
+  tlbm_options opt_{};
+  std::string workdir_;
+  int q_ = 19;
+  bool ref_arith_ = true;
+  int store_ = kStoreF32;
+  int sb_ = 4;  // bytes per stored population
+  int ob_ = 4;  // bytes per output value
+  int64_t n_ = 0;
+  int cut_size_ = 0;
+  bool has_type5_ = false;
+  bool identity_order_ = true;
+  std::vector<int32_t> order_;  // output position -> global node (partition-major)
+  DevProblem pb_{};
+  Launch launch_{};
+  cudaStream_t stream_ = nullptr;
+
+  uint8_t* d_type_ = nullptr;
+  void* d_f_[2] = {nullptr, nullptr};  // [0] = fEven, [1] = fOdd
+  void* d_macro_[4] = {nullptr, nullptr, nullptr, nullptr};
+  void* d_force_[3] = {nullptr, nullptr, nullptr};
+  void* d_avg_[4] = {nullptr, nullptr, nullptr, nullptr};
+  void* d_uyq_[2] = {nullptr, nullptr};
+  void* d_stage_ = nullptr;
+  int32_t* d_order_ = nullptr;
+  double* d_partial_ = nullptr;
+  double* d_mass_ = nullptr;
+  void* h_pinned_ = nullptr;
+  cudaGraphExec_t graph_[2] = {nullptr, nullptr};
+
+  int last_src_ = -1, last_dst_ = -1;
+  bool outputs_fresh_ = false;
+  int dump_num_ = 0;
+  int64_t steps_ = 0;
+  int64_t launches_ = 0;
+};
+
+}  // namespace tlbm

@@ -1,0 +1,68 @@
+// grid.cuh -- lattice geometry on the device and the periodic neighbour arithmetic.
+//
+// Populations are stored structure-of-arrays, f[speed][z][y][x] (x fastest), so a warp's 32
+// consecutive x cells read and write 32 consecutive values of one speed.  The stream step is a
+// pull: cell c gathers speed i from cell c - e_i, with periodic wrap on all three axes exactly
+// like get_tgt_index (src/TLBM_Partition.cpp:691-712): the reference pushes to c + e_i, so
+// pulling from c - e_i moves the same values.
+#pragma once
+
+#include <cstdint>
+
+#include "lattice.cuh"
+
+namespace tlbm {
+
+struct DevProblem {
+  int nx, ny, nz;
+  int nxy;         // nx*ny
+  int64_t n;       // nx*ny*nz (< 2^31 so cell offsets fit in int)
+  const uint8_t* nd_type;
+  double omega, cs, u_bc, rho_bc;  // the parsed `real` values, held exactly
+  int dynamics;
+  int has_type5;
+};
+
+// offsets of a cell and its periodic neighbours along each axis
+struct Nbr {
+  int x0, xm, xp;  // x, x-1, x+1 (wrapped)
+  int y0, ym, yp;  // row offsets y*nx, (y-1)*nx, (y+1)*nx (wrapped)
+  int z0, zm, zp;  // plane offsets z*nxy, ...
+
+  TLBM_HD Nbr(int x, int y, int z, int nx, int ny, int nz, int nxy) {
+    x0 = x;
+    xm = (x == 0) ? nx - 1 : x - 1;
+    xp = (x == nx - 1) ? 0 : x + 1;
+    y0 = y * nx;
+    ym = ((y == 0) ? ny - 1 : y - 1) * nx;
+    yp = ((y == ny - 1) ? 0 : y + 1) * nx;
+    z0 = z * nxy;
+    zm = ((z == 0) ? nz - 1 : z - 1) * nxy;
+    zp = ((z == nz - 1) ? 0 : z + 1) * nxy;
+  }
+  TLBM_HD int self() const { return x0 + y0 + z0; }
+  // cell c - e_i (where speed i streams from)
+  template <class L>
+  TLBM_HD int from(int i) const {
+    const int ex = L::ex(i), ey = L::ey(i), ez = L::ez(i);
+    return (ex > 0 ? xm : (ex < 0 ? xp : x0)) + (ey > 0 ? ym : (ey < 0 ? yp : y0)) +
+           (ez > 0 ? zm : (ez < 0 ? zp : z0));
+  }
+  // cell c + e_i (where speed i streams to: the reference's adj[c*Q+i])
+  template <class L>
+  TLBM_HD int to(int i) const {
+    const int ex = L::ex(i), ey = L::ey(i), ez = L::ez(i);
+    return (ex > 0 ? xp : (ex < 0 ? xm : x0)) + (ey > 0 ? yp : (ey < 0 ? ym : y0)) +
+           (ez > 0 ? zp : (ez < 0 ? zm : z0));
+  }
+};
+
+// cell index -> (x, y, z)
+TLBM_HD void decompose(int c, int nx, int nxy, int& x, int& y, int& z) {
+  z = c / nxy;
+  const int r = c - z * nxy;
+  y = r / nx;
+  x = r - y * nx;
+}
+
+}  // namespace tlbm

@@ -1,0 +1,74 @@
+// kernels.h -- host-side launch interface of the CUDA kernels (no CUDA types beyond the stream).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "grid.cuh"
+
+namespace tlbm {
+
+// storage kinds of the population arrays
+enum StoreKind : int { kStoreF64 = 0, kStoreF32 = 1, kStoreBF16 = 2, kStoreF16 = 3 };
+inline int store_bytes(int k) { return k == kStoreF64 ? 8 : (k == kStoreF32 ? 4 : 2); }
+
+struct StepArgs {
+  DevProblem pb;
+  const void* src;   // populations after the previous step's collision (pull source)
+  void* dst;         // populations after this step's collision
+  void* avg[4];      // time-average sums of ux, uy, uz, rho (null when off)
+  int time_avg;
+  const void* uyq_cur;   // uy of nodes 0..Q-1 in this step   (type-5 quirk, see ref::set_uz)
+  const void* uyq_prev;  // uy of nodes 0..Q-1 in the previous step
+  void* macro[4];        // fused macroscopic output (fast kernels; null when not wanted)
+};
+
+struct Launch {
+  int bx = 32, by = 4;
+  cudaStream_t stream = nullptr;
+};
+
+// ---- reference arithmetic (bit-identical to the CPU reference); R = double or float
+cudaError_t launch_step_ref(int q, int rbytes, const StepArgs& a, const Launch& l);
+// macroscopic values of every node, recomputed from the step's pull source: out[4] in R
+cudaError_t launch_macros_ref(int q, int rbytes, const DevProblem& pb, const void* src,
+                              void* const out[4], const Launch& l);
+// uy of nodes 0..min(Q,n)-1 (the type-5 quirk) from the pull source
+cudaError_t launch_quirk_uy_ref(int q, int rbytes, const DevProblem& pb, const void* src,
+                                void* uy_out, const Launch& l);
+// calc_force on the post-stream populations (pull of `dst`): out[3] in R
+cudaError_t launch_force_ref(int q, int rbytes, const DevProblem& pb, const void* dst,
+                             void* const out[3], const Launch& l);
+
+// ---- fast arithmetic (FMA, reassociated); storage kind k, compute in double (f64) or float
+cudaError_t launch_step_fast(int q, int store, const StepArgs& a, const Launch& l);
+cudaError_t launch_macros_fast(int q, int store, const DevProblem& pb, const void* src,
+                               void* const out[4], const Launch& l);
+cudaError_t launch_force_fast(int q, int store, const DevProblem& pb, const void* dst,
+                              void* const out[3], const Launch& l);
+
+// ---- storage-generic utilities
+// f_i = w_i * rho in both buffers (initialize_data_arrays, src/TLBM_Partition.cpp:448-479);
+// for the 16-bit kinds the stored value is f_i - w_i.
+cudaError_t launch_init_uniform(int q, int store, const DevProblem& pb, void* f, double rho,
+                                const Launch& l);
+// f = feq(u, rho) per node, placed so that the first pull reads it back at its own node
+// (restart initialisation, src/TLBM_Partition.cpp:527-532)
+cudaError_t launch_init_equilibrium(int q, int store, const DevProblem& pb, void* f,
+                                    const void* const macro[4], int macro_bytes,
+                                    const Launch& l);
+// populations in the reference's AoS layout; post_stream=1 gathers c - e_i
+cudaError_t launch_to_aos(int q, int store, const DevProblem& pb, const void* f, int post_stream,
+                          void* out, int out_bytes, const Launch& l);
+cudaError_t launch_adjacency(int q, const DevProblem& pb, int32_t* out, const Launch& l);
+// deterministic FP64 sum of all populations: partial sums per block into `partial`
+// (nblocks doubles), then one block folds them into *out
+int mass_blocks(const DevProblem& pb);
+cudaError_t launch_mass(int q, int store, const DevProblem& pb, const void* f, double* partial,
+                        int nblocks, double* out, const Launch& l);
+// out[k] = in[order[k]] for element size `bytes`
+cudaError_t launch_gather(const void* in, const int32_t* order, int64_t n, int bytes, void* out,
+                          const Launch& l);
+
+}  // namespace tlbm

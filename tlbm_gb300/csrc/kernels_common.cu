@@ -1,0 +1,264 @@
+// kernels_common.cu -- storage-generic kernels: initialisation, layout export, neighbour-table
+// export, the deterministic FP64 mass reduction and the partition-order gather.
+#include "grid.cuh"
+#include "kernels.h"
+#include "physics_ref.cuh"
+#include "storage.cuh"
+
+namespace tlbm {
+namespace {
+
+constexpr int kThreads = 256;
+
+// grid-stride over all cells
+#define TLBM_FOR_CELLS(c, n)                                                                \
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < (n);                 \
+       c += (int64_t)gridDim.x * blockDim.x)
+
+int blocks_for(int64_t n) {
+  int64_t b = (n + kThreads - 1) / kThreads;
+  if (b > 152 * 16) b = 152 * 16;
+  if (b < 1) b = 1;
+  return static_cast<int>(b);
+}
+
+template <class L, int K>
+__global__ void k_init_uniform(DevProblem pb, typename Store<K>::T* f, double rho) {
+  using S = Store<K>;
+  using C = typename S::C;
+  const size_t n = static_cast<size_t>(pb.n);
+  TLBM_FOR_CELLS(c, pb.n) {
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) {
+      if constexpr (S::kShifted) {
+        const C w = weight<L, float>(i);
+        f[i * n + c] = S::save(w * static_cast<C>(rho), w);
+      } else {
+        // w[spd]*rho in `real` (src/TLBM_Partition.cpp:462-463)
+        f[i * n + c] = weight<L, C>(i) * static_cast<C>(rho);
+      }
+    }
+  }
+}
+
+// restart: f = feq(u, rho) of each node (load_restart_data, src/TLBM_Partition.cpp:527-532),
+// written to c - e_i so that the first pull returns it at node c
+template <class L, int K, class M>
+__global__ void k_init_equilibrium(DevProblem pb, typename Store<K>::T* f, const M* ux,
+                                   const M* uy, const M* uz, const M* rho) {
+  using S = Store<K>;
+  using C = typename S::C;
+  const size_t n = static_cast<size_t>(pb.n);
+  TLBM_FOR_CELLS(c, pb.n) {
+    int x, y, z;
+    decompose(static_cast<int>(c), pb.nx, pb.nxy, x, y, z);
+    const Nbr nb(x, y, z, pb.nx, pb.ny, pb.nz, pb.nxy);
+    C feq[L::Q];
+    ref::equilibrium<L, C>(static_cast<C>(ux[c]), static_cast<C>(uy[c]), static_cast<C>(uz[c]),
+                           static_cast<C>(rho[c]), feq);
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) {
+      const C w = S::kShifted ? weight<L, float>(i) : C(0);
+      f[i * n + nb.from<L>(i)] = S::save(feq[i], w);
+    }
+  }
+}
+
+template <class L, int K, class O>
+__global__ void k_to_aos(DevProblem pb, const typename Store<K>::T* f, int post_stream, O* out) {
+  using S = Store<K>;
+  using C = typename S::C;
+  const size_t n = static_cast<size_t>(pb.n);
+  TLBM_FOR_CELLS(c, pb.n) {
+    int x, y, z;
+    decompose(static_cast<int>(c), pb.nx, pb.nxy, x, y, z);
+    const Nbr nb(x, y, z, pb.nx, pb.ny, pb.nz, pb.nxy);
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) {
+      const int src = post_stream ? nb.from<L>(i) : static_cast<int>(c);
+      const C w = S::kShifted ? weight<L, float>(i) : C(0);
+      out[c * L::Q + i] = static_cast<O>(S::load(f[i * n + src], w));
+    }
+  }
+}
+
+template <class L>
+__global__ void k_adjacency(DevProblem pb, int32_t* out) {
+  TLBM_FOR_CELLS(c, pb.n) {
+    int x, y, z;
+    decompose(static_cast<int>(c), pb.nx, pb.nxy, x, y, z);
+    const Nbr nb(x, y, z, pb.nx, pb.ny, pb.nz, pb.nxy);
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) out[c * L::Q + i] = nb.to<L>(i);
+  }
+}
+
+// block-level deterministic double sum (fixed shuffle tree, fixed smem tree)
+__device__ double block_sum(double v) {
+  __shared__ double warp_part[kThreads / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) warp_part[wid] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (wid == 0) {
+    r = lane < kThreads / 32 ? warp_part[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+  }
+  return r;  // valid in thread 0
+}
+
+template <class L, int K>
+__global__ void __launch_bounds__(kThreads) k_mass_partial(DevProblem pb,
+                                                           const typename Store<K>::T* f,
+                                                           double* partial) {
+  using S = Store<K>;
+  const size_t n = static_cast<size_t>(pb.n);
+  double acc = 0.0;
+  TLBM_FOR_CELLS(c, pb.n) {
+    double cell = 0.0;
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) {
+      if constexpr (S::kShifted)
+        cell += static_cast<double>(weight<L, float>(i)) + static_cast<double>(f[i * n + c]);
+      else
+        cell += static_cast<double>(f[i * n + c]);
+    }
+    acc += cell;
+  }
+  const double b = block_sum(acc);
+  if (threadIdx.x == 0) partial[blockIdx.x] = b;
+}
+
+__global__ void __launch_bounds__(kThreads) k_mass_final(const double* partial, int nb,
+                                                         double* out) {
+  double acc = 0.0;
+  for (int k = threadIdx.x; k < nb; k += kThreads) acc += partial[k];
+  const double b = block_sum(acc);
+  if (threadIdx.x == 0) *out = b;
+}
+
+template <class E>
+__global__ void k_gather(const E* in, const int32_t* order, int64_t n, E* out) {
+  TLBM_FOR_CELLS(k, n) out[k] = in[order[k]];
+}
+
+template <template <class, int> class Fn, class... A>
+cudaError_t by_q_store(int q, int store, A&&... a) {
+#define TLBM_CASE_K(QQ, KK) \
+  if (q == QQ && store == KK) return Fn<Lattice<QQ>, KK>::run(a...);
+  TLBM_CASE_K(15, kStoreF64) TLBM_CASE_K(15, kStoreF32) TLBM_CASE_K(15, kStoreBF16)
+  TLBM_CASE_K(15, kStoreF16) TLBM_CASE_K(19, kStoreF64) TLBM_CASE_K(19, kStoreF32)
+  TLBM_CASE_K(19, kStoreBF16) TLBM_CASE_K(19, kStoreF16) TLBM_CASE_K(27, kStoreF64)
+  TLBM_CASE_K(27, kStoreF32) TLBM_CASE_K(27, kStoreBF16) TLBM_CASE_K(27, kStoreF16)
+#undef TLBM_CASE_K
+  return cudaErrorInvalidValue;
+}
+
+template <class L, int K>
+struct InitUniform {
+  static cudaError_t run(const DevProblem& pb, void* f, double rho, const Launch& l) {
+    k_init_uniform<L, K><<<blocks_for(pb.n), kThreads, 0, l.stream>>>(
+        pb, static_cast<typename Store<K>::T*>(f), rho);
+    return cudaGetLastError();
+  }
+};
+
+template <class L, int K>
+struct InitEq {
+  static cudaError_t run(const DevProblem& pb, void* f, const void* const* m, int mb,
+                         const Launch& l) {
+    auto* ff = static_cast<typename Store<K>::T*>(f);
+    if (mb == 8)
+      k_init_equilibrium<L, K, double><<<blocks_for(pb.n), kThreads, 0, l.stream>>>(
+          pb, ff, static_cast<const double*>(m[0]), static_cast<const double*>(m[1]),
+          static_cast<const double*>(m[2]), static_cast<const double*>(m[3]));
+    else
+      k_init_equilibrium<L, K, float><<<blocks_for(pb.n), kThreads, 0, l.stream>>>(
+          pb, ff, static_cast<const float*>(m[0]), static_cast<const float*>(m[1]),
+          static_cast<const float*>(m[2]), static_cast<const float*>(m[3]));
+    return cudaGetLastError();
+  }
+};
+
+template <class L, int K>
+struct ToAos {
+  static cudaError_t run(const DevProblem& pb, const void* f, int post, void* out, int ob,
+                         const Launch& l) {
+    auto* ff = static_cast<const typename Store<K>::T*>(f);
+    if (ob == 8)
+      k_to_aos<L, K, double><<<blocks_for(pb.n), kThreads, 0, l.stream>>>(
+          pb, ff, post, static_cast<double*>(out));
+    else
+      k_to_aos<L, K, float><<<blocks_for(pb.n), kThreads, 0, l.stream>>>(
+          pb, ff, post, static_cast<float*>(out));
+    return cudaGetLastError();
+  }
+};
+
+template <class L, int K>
+struct Mass {
+  static cudaError_t run(const DevProblem& pb, const void* f, double* partial, int nb,
+                         double* out, const Launch& l) {
+    k_mass_partial<L, K><<<nb, kThreads, 0, l.stream>>>(
+        pb, static_cast<const typename Store<K>::T*>(f), partial);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_mass_final<<<1, kThreads, 0, l.stream>>>(partial, nb, out);
+    return cudaGetLastError();
+  }
+};
+
+}  // namespace
+
+cudaError_t launch_init_uniform(int q, int store, const DevProblem& pb, void* f, double rho,
+                                const Launch& l) {
+  return by_q_store<InitUniform>(q, store, pb, f, rho, l);
+}
+
+cudaError_t launch_init_equilibrium(int q, int store, const DevProblem& pb, void* f,
+                                    const void* const macro[4], int macro_bytes,
+                                    const Launch& l) {
+  return by_q_store<InitEq>(q, store, pb, f, macro, macro_bytes, l);
+}
+
+cudaError_t launch_to_aos(int q, int store, const DevProblem& pb, const void* f, int post_stream,
+                          void* out, int out_bytes, const Launch& l) {
+  return by_q_store<ToAos>(q, store, pb, f, post_stream, out, out_bytes, l);
+}
+
+cudaError_t launch_adjacency(int q, const DevProblem& pb, int32_t* out, const Launch& l) {
+  const int b = blocks_for(pb.n);
+  switch (q) {
+    case 15: k_adjacency<Lattice<15>><<<b, kThreads, 0, l.stream>>>(pb, out); break;
+    case 19: k_adjacency<Lattice<19>><<<b, kThreads, 0, l.stream>>>(pb, out); break;
+    case 27: k_adjacency<Lattice<27>><<<b, kThreads, 0, l.stream>>>(pb, out); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+int mass_blocks(const DevProblem& pb) { return blocks_for(pb.n); }
+
+cudaError_t launch_mass(int q, int store, const DevProblem& pb, const void* f, double* partial,
+                        int nblocks, double* out, const Launch& l) {
+  return by_q_store<Mass>(q, store, pb, f, partial, nblocks, out, l);
+}
+
+cudaError_t launch_gather(const void* in, const int32_t* order, int64_t n, int bytes, void* out,
+                          const Launch& l) {
+  const int b = blocks_for(n);
+  if (bytes == 8)
+    k_gather<double><<<b, kThreads, 0, l.stream>>>(static_cast<const double*>(in), order, n,
+                                                  static_cast<double*>(out));
+  else if (bytes == 4)
+    k_gather<float><<<b, kThreads, 0, l.stream>>>(static_cast<const float*>(in), order, n,
+                                                 static_cast<float*>(out));
+  else
+    return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+}  // namespace tlbm

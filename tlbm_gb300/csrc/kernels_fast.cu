@@ -1,0 +1,284 @@
+// kernels_fast.cu -- the fused stream-collide step for throughput (FMA, reassociated sums).
+//
+// Same data flow as kernels_ref.cu -- one thread per cell, pull Q populations from c - e_i,
+// node-type branch, collide in registers, store at c -- for every storage kind of
+// storage.cuh.  Solid nodes move the raw stored values (bounce-back needs no arithmetic, and
+// opposite speeds share a weight, so the f - w shift of 16-bit storage carries over unchanged).
+#include "kernels.h"
+#include "physics_fast.cuh"
+#include "storage.cuh"
+
+namespace tlbm {
+namespace {
+
+template <class L, int K>
+__device__ __forceinline__ void load_cell(const typename Store<K>::T* __restrict__ src, size_t n,
+                                          const Nbr& nb, typename Store<K>::T (&raw)[L::Q]) {
+#pragma unroll
+  for (int i = 0; i < L::Q; ++i) raw[i] = __ldg(src + i * n + nb.from<L>(i));
+}
+
+template <class L, int K>
+__device__ __forceinline__ void unpack(const typename Store<K>::T (&raw)[L::Q],
+                                       typename Store<K>::C (&f)[L::Q]) {
+  using S = Store<K>;
+  using C = typename S::C;
+#pragma unroll
+  for (int i = 0; i < L::Q; ++i) f[i] = S::load(raw[i], fast::wgt<L, C>(i));
+}
+
+// node macroscopic values as the reference holds them after processing the node
+template <class L, class C>
+__device__ __forceinline__ void node_macros(uint8_t t, const C (&f)[L::Q], C u_bc, C rho_bc,
+                                            C& rho, C& ux, C& uy, C& uz) {
+  if (t == kSolid) {
+    rho = fast::density<L, C>(f);
+    ux = uy = uz = C(0);
+  } else if (t == kInlet) {
+    rho = fast::inlet_rho<L, C>(f, C(1) / (C(1) - u_bc));
+    ux = uy = C(0);
+    uz = u_bc;
+  } else {
+    fast::moments<L, C>(f, rho, ux, uy, uz);
+    if (t == kOutlet) {
+      rho = rho_bc;
+      uz = fast::outlet_uz<L, C>(f, C(1) / rho_bc);
+    }
+  }
+}
+
+template <class L, int K, bool kSmag>
+__global__ void __launch_bounds__(128) k_step_fast(StepArgs a) {
+  using S = Store<K>;
+  using C = typename S::C;
+  using T = typename S::T;
+  const DevProblem& pb = a.pb;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= pb.nx || y >= pb.ny) return;
+  const Nbr nb(x, y, z, pb.nx, pb.ny, pb.nz, pb.nxy);
+  const int c = nb.self();
+  const size_t n = static_cast<size_t>(pb.n);
+  const T* __restrict__ src = static_cast<const T*>(a.src);
+  T* __restrict__ dst = static_cast<T*>(a.dst);
+
+  T raw[L::Q];
+  load_cell<L, K>(src, n, nb, raw);
+  const uint8_t t = pb.nd_type[c];
+  C rho = 0, ux = 0, uy = 0, uz = 0;
+  if (t == kSolid) {
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) dst[i * n + c] = raw[L::bb(i)];
+    if (a.time_avg) {
+      C f[L::Q];
+      unpack<L, K>(raw, f);
+      rho = fast::density<L, C>(f);
+    }
+  } else {
+    C f[L::Q];
+    unpack<L, K>(raw, f);
+    const C u_bc = static_cast<C>(pb.u_bc);
+    node_macros<L, C>(t, f, u_bc, static_cast<C>(pb.rho_bc), rho, ux, uy, uz);
+    if (pb.has_type5 && t == kMovingWall) {
+      const C* cur = static_cast<const C*>(a.uyq_cur);
+      const C* prev = static_cast<const C*>(a.uyq_prev);
+#pragma unroll
+      for (int i = 0; i < L::Q; ++i) {
+        const C uyq = i <= c ? cur[i] : prev[i];
+        f[i] += C(3) * rho * fast::wgt<L, C>(i) *
+                (C(L::ez(i)) * (u_bc - uz) - C(L::ex(i)) * ux - C(L::ey(i)) * uyq);
+      }
+    }
+    C feq[L::Q];
+    fast::equilibrium<L, C>(rho, ux, uy, uz, feq);
+    if (t == kInlet) fast::nebb<L, C, true>(f, feq);
+    if (t == kOutlet) fast::nebb<L, C, false>(f, feq);
+    if (pb.dynamics == 1) {
+      C om = static_cast<C>(pb.omega);
+      if constexpr (kSmag) {
+        const C nu = (C(1) / om - C(0.5)) / C(3);
+        om = fast::smagorinsky_omega<L, C>(f, feq, static_cast<C>(pb.cs), nu);
+      }
+      fast::relax<L, C>(f, feq, om);
+    }
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) dst[i * n + c] = S::save(f[i], fast::wgt<L, C>(i));
+  }
+  if (a.time_avg) {
+    C* const* avg = reinterpret_cast<C* const*>(a.avg);
+    avg[0][c] += ux;
+    avg[1][c] += uy;
+    avg[2][c] += uz;
+    avg[3][c] += rho;
+  }
+}
+
+template <class L, int K>
+__global__ void __launch_bounds__(128) k_macros_fast(DevProblem pb,
+                                                    const typename Store<K>::T* __restrict__ src,
+                                                    typename Store<K>::C* ux_o,
+                                                    typename Store<K>::C* uy_o,
+                                                    typename Store<K>::C* uz_o,
+                                                    typename Store<K>::C* rho_o) {
+  using C = typename Store<K>::C;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= pb.nx || y >= pb.ny) return;
+  const Nbr nb(x, y, z, pb.nx, pb.ny, pb.nz, pb.nxy);
+  const int c = nb.self();
+  typename Store<K>::T raw[L::Q];
+  load_cell<L, K>(src, static_cast<size_t>(pb.n), nb, raw);
+  C f[L::Q];
+  unpack<L, K>(raw, f);
+  C rho, ux, uy, uz;
+  node_macros<L, C>(pb.nd_type[c], f, static_cast<C>(pb.u_bc), static_cast<C>(pb.rho_bc), rho, ux,
+                    uy, uz);
+  ux_o[c] = ux;
+  uy_o[c] = uy;
+  uz_o[c] = uz;
+  rho_o[c] = rho;
+}
+
+template <class L, int K>
+__global__ void k_quirk_fast(DevProblem pb, const typename Store<K>::T* __restrict__ src,
+                             typename Store<K>::C* uy_out) {
+  using C = typename Store<K>::C;
+  const int c = threadIdx.x;
+  if (c >= L::Q || c >= pb.n) return;
+  int x, y, z;
+  decompose(c, pb.nx, pb.nxy, x, y, z);
+  const Nbr nb(x, y, z, pb.nx, pb.ny, pb.nz, pb.nxy);
+  typename Store<K>::T raw[L::Q];
+  load_cell<L, K>(src, static_cast<size_t>(pb.n), nb, raw);
+  C f[L::Q];
+  unpack<L, K>(raw, f);
+  C rho, ux, uy, uz;
+  node_macros<L, C>(pb.nd_type[c], f, static_cast<C>(pb.u_bc), static_cast<C>(pb.rho_bc), rho, ux,
+                    uy, uz);
+  uy_out[c] = uy;
+}
+
+template <class L, int K>
+__global__ void __launch_bounds__(128) k_force_fast(DevProblem pb,
+                                                   const typename Store<K>::T* __restrict__ f,
+                                                   typename Store<K>::C* fx_o,
+                                                   typename Store<K>::C* fy_o,
+                                                   typename Store<K>::C* fz_o) {
+  using S = Store<K>;
+  using C = typename S::C;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= pb.nx || y >= pb.ny) return;
+  const Nbr nb(x, y, z, pb.nx, pb.ny, pb.nz, pb.nxy);
+  const int c = nb.self();
+  const size_t n = static_cast<size_t>(pb.n);
+  C fx = 0, fy = 0, fz = 0;
+  if (pb.nd_type[c] == kSolid) {
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) {
+      const int g = nb.to<L>(i);
+      if (pb.nd_type[g] != kFluid) continue;
+      const int b = L::bb(i);
+      int gx, gy, gz;
+      decompose(g, pb.nx, pb.nxy, gx, gy, gz);
+      const Nbr ng(gx, gy, gz, pb.nx, pb.ny, pb.nz, pb.nxy);
+      const C f1 = S::load(f[i * n + nb.from<L>(i)], fast::wgt<L, C>(i));
+      const C f2 = S::load(f[b * n + ng.from<L>(b)], fast::wgt<L, C>(b));
+      const C s = f1 + f2;
+      fx += C(L::ex(b)) * s;
+      fy += C(L::ey(b)) * s;
+      fz += C(L::ez(b)) * s;
+    }
+  }
+  fx_o[c] = fx;
+  fy_o[c] = fy;
+  fz_o[c] = fz;
+}
+
+dim3 grid_of(const DevProblem& pb, const Launch& l) {
+  return dim3((pb.nx + l.bx - 1) / l.bx, (pb.ny + l.by - 1) / l.by, pb.nz);
+}
+
+template <class L, int K>
+cudaError_t step_lk(const StepArgs& a, const Launch& l) {
+  const dim3 g = grid_of(a.pb, l), b(l.bx, l.by, 1);
+  if (a.pb.cs > 0)
+    k_step_fast<L, K, true><<<g, b, 0, l.stream>>>(a);
+  else
+    k_step_fast<L, K, false><<<g, b, 0, l.stream>>>(a);
+  return cudaGetLastError();
+}
+
+template <class L, int K>
+cudaError_t macros_lk(const DevProblem& pb, const void* src, void* const out[4], const Launch& l) {
+  using C = typename Store<K>::C;
+  const dim3 g = grid_of(pb, l), b(l.bx, l.by, 1);
+  k_macros_fast<L, K><<<g, b, 0, l.stream>>>(
+      pb, static_cast<const typename Store<K>::T*>(src), static_cast<C*>(out[0]),
+      static_cast<C*>(out[1]), static_cast<C*>(out[2]), static_cast<C*>(out[3]));
+  return cudaGetLastError();
+}
+
+template <class L, int K>
+cudaError_t quirk_lk(const DevProblem& pb, const void* src, void* out, const Launch& l) {
+  using C = typename Store<K>::C;
+  k_quirk_fast<L, K><<<1, 32, 0, l.stream>>>(pb, static_cast<const typename Store<K>::T*>(src),
+                                              static_cast<C*>(out));
+  return cudaGetLastError();
+}
+
+template <class L, int K>
+cudaError_t force_lk(const DevProblem& pb, const void* f, void* const out[3], const Launch& l) {
+  using C = typename Store<K>::C;
+  const dim3 g = grid_of(pb, l), b(l.bx, l.by, 1);
+  k_force_fast<L, K><<<g, b, 0, l.stream>>>(pb, static_cast<const typename Store<K>::T*>(f),
+                                             static_cast<C*>(out[0]), static_cast<C*>(out[1]),
+                                             static_cast<C*>(out[2]));
+  return cudaGetLastError();
+}
+
+#define TLBM_DISPATCH(FN, q, store, ...)                                            \
+  do {                                                                              \
+    switch (q * 10 + store) {                                                       \
+      case 150: return FN<Lattice<15>, kStoreF64>(__VA_ARGS__);                     \
+      case 151: return FN<Lattice<15>, kStoreF32>(__VA_ARGS__);                     \
+      case 152: return FN<Lattice<15>, kStoreBF16>(__VA_ARGS__);                    \
+      case 153: return FN<Lattice<15>, kStoreF16>(__VA_ARGS__);                     \
+      case 190: return FN<Lattice<19>, kStoreF64>(__VA_ARGS__);                     \
+      case 191: return FN<Lattice<19>, kStoreF32>(__VA_ARGS__);                     \
+      case 192: return FN<Lattice<19>, kStoreBF16>(__VA_ARGS__);                    \
+      case 193: return FN<Lattice<19>, kStoreF16>(__VA_ARGS__);                     \
+      case 270: return FN<Lattice<27>, kStoreF64>(__VA_ARGS__);                     \
+      case 271: return FN<Lattice<27>, kStoreF32>(__VA_ARGS__);                     \
+      case 272: return FN<Lattice<27>, kStoreBF16>(__VA_ARGS__);                    \
+      case 273: return FN<Lattice<27>, kStoreF16>(__VA_ARGS__);                     \
+      default: return cudaErrorInvalidValue;                                        \
+    }                                                                               \
+  } while (0)
+
+}  // namespace
+
+cudaError_t launch_step_fast(int q, int store, const StepArgs& a, const Launch& l) {
+  if (a.pb.has_type5) {
+    cudaError_t e = [&]() -> cudaError_t {
+      TLBM_DISPATCH(quirk_lk, q, store, a.pb, a.src, const_cast<void*>(a.uyq_cur), l);
+    }();
+    if (e != cudaSuccess) return e;
+  }
+  TLBM_DISPATCH(step_lk, q, store, a, l);
+}
+
+cudaError_t launch_macros_fast(int q, int store, const DevProblem& pb, const void* src,
+                               void* const out[4], const Launch& l) {
+  TLBM_DISPATCH(macros_lk, q, store, pb, src, out, l);
+}
+
+cudaError_t launch_force_fast(int q, int store, const DevProblem& pb, const void* dst,
+                              void* const out[3], const Launch& l) {
+  TLBM_DISPATCH(force_lk, q, store, pb, dst, out, l);
+}
+
+}  // namespace tlbm

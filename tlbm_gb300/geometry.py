@@ -221,33 +221,53 @@ def random_sphere_pack(
     centres = []
     n_solid = 0
     tries = 0
+    # candidate spheres are drawn in seeded batches; overlap tests look only at the accepted
+    # spheres hashed into the 27 grid cells (edge 2*r_max) around the candidate
+    h = 2.0 * r_max
+    gx, gy, gz = max(1, int(nx // h)), max(1, int(ny // h)), max(1, int(math.ceil(nz / h)))
+    sx, sy, sz = nx / gx, ny / gy, nz / gz
+    grid: dict = {}
+    batch = 65536
     while n_solid < target and tries < max_tries:
-        tries += 1
-        r = rng.uniform(r_min, r_max)
-        c = np.array([rng.uniform(0, nx), rng.uniform(0, ny),
-                      rng.uniform(z_margin, nz - 1 - z_margin)])
-        ok = True
-        for (c2, r2) in centres:
-            d = np.abs(c - c2)
-            d[0] = min(d[0], nx - d[0])
-            d[1] = min(d[1], ny - d[1])
-            if float(np.sqrt((d**2).sum())) < r + r2:
-                ok = False
+        rs = rng.uniform(r_min, r_max, batch)
+        cs = np.stack([rng.uniform(0, nx, batch), rng.uniform(0, ny, batch),
+                       rng.uniform(z_margin, nz - 1 - z_margin, batch)], axis=1)
+        for k in range(batch):
+            if n_solid >= target or tries >= max_tries:
                 break
-        if not ok:
-            continue
-        centres.append((c, r))
-        rr = int(math.ceil(r))
-        zs = np.arange(max(0, int(math.floor(c[2] - rr))), min(nz, int(math.ceil(c[2] + rr)) + 1))
-        ys = np.arange(int(math.floor(c[1] - rr)), int(math.ceil(c[1] + rr)) + 1)
-        xs = np.arange(int(math.floor(c[0] - rr)), int(math.ceil(c[0] + rr)) + 1)
-        dz = (zs - c[2])[:, None, None]
-        dy = (ys - c[1])[None, :, None]
-        dxx = (xs - c[0])[None, None, :]
-        ball = (dxx**2 + dy**2 + dz**2) < r * r
-        sub = solid[np.ix_(zs, ys % ny, xs % nx)]
-        n_solid += int((ball & ~sub).sum())
-        solid[np.ix_(zs, ys % ny, xs % nx)] = sub | ball
+            tries += 1
+            r = float(rs[k])
+            cx, cy, cz = float(cs[k, 0]), float(cs[k, 1]), float(cs[k, 2])
+            ix, iy, iz = int(cx / sx) % gx, int(cy / sy) % gy, min(int(cz / sz), gz - 1)
+            ok = True
+            for dz in (-1, 0, 1):
+                jz = iz + dz
+                if jz < 0 or jz >= gz:
+                    continue
+                for dy in (-1, 0, 1):
+                    jy = (iy + dy) % gy
+                    for dx in (-1, 0, 1):
+                        for (qx, qy, qz, qr) in grid.get(((ix + dx) % gx, jy, jz), ()):
+                            ddx = abs(cx - qx)
+                            ddx = min(ddx, nx - ddx)
+                            ddy = abs(cy - qy)
+                            ddy = min(ddy, ny - ddy)
+                            ddz = cz - qz
+                            if ddx * ddx + ddy * ddy + ddz * ddz < (r + qr) ** 2:
+                                ok = False
+                                break
+                        if not ok:
+                            break
+                    if not ok:
+                        break
+                if not ok:
+                    break
+            if not ok:
+                continue
+            grid.setdefault((ix, iy, iz), []).append((cx, cy, cz, r))
+            c = np.array([cx, cy, cz])
+            n_solid += _rasterise_sphere(solid, c, r, nx, ny, nz)
+            centres.append((c, r))
     nd = np.zeros((nz, ny, nx), dtype=np.int32)
     nd[0] = INLET
     nd[nz - 1] = OUTLET
@@ -260,8 +280,26 @@ def random_sphere_pack(
         "mean_diameter": g.lo,
         "porosity": 1.0 - float(solid.sum()) / solid.size,
         "seed": seed,
+        "tries": tries,
     }
     return g
+
+
+def _rasterise_sphere(solid, c, r, nx, ny, nz) -> int:
+    """Mark |p - c|^2 < r^2 (periodic in x, y) solid; returns the number of new solid nodes."""
+    rr = int(math.ceil(r))
+    zs = np.arange(max(0, int(math.floor(c[2] - rr))), min(nz, int(math.ceil(c[2] + rr)) + 1))
+    ys = np.arange(int(math.floor(c[1] - rr)), int(math.ceil(c[1] + rr)) + 1)
+    xs = np.arange(int(math.floor(c[0] - rr)), int(math.ceil(c[0] + rr)) + 1)
+    dz = (zs - c[2])[:, None, None]
+    dy = (ys - c[1])[None, :, None]
+    dxx = (xs - c[0])[None, None, :]
+    ball = (dxx**2 + dy**2 + dz**2) < r * r
+    idx = np.ix_(zs, ys % ny, xs % nx)
+    sub = solid[idx]
+    added = int((ball & ~sub).sum())
+    solid[idx] = sub | ball
+    return added
 
 
 def sphere_in_box(nx, ny, nz, r, xc, yc, zc, walls=True) -> Geometry:
