@@ -182,6 +182,21 @@ tlbm_status tlbm_mass(tlbm_handle* h, double* mass);
 /* Number of kernels this handle has launched since creation. */
 int64_t tlbm_kernel_launches(const tlbm_handle* h);
 
+/* ---- allocation-free mass reduction --------------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device memory while they
+ * run -- applications that reserve the whole GPU for their own memory pool up front, or loops
+ * whose policy forbids allocation after start-up -- this computes what tlbm_mass computes, the
+ * FP64 sum of all populations, without any allocation: the caller passes the populations
+ * (device memory, the engine's layout f[speed * n_cells + cell] in the storage type of
+ * `precision`, 16-bit kinds holding f - w) and `mass` (device memory, one double), and the
+ * partial sums go to a static device array of 512 KiB that every GPU loading the library keeps
+ * until exit.  Limit: n_cells <= 67108864 (65536 partials of 1024 cells); larger inputs return
+ * TLBM_ERR_OUT_OF_RANGE and launch nothing.  The first call on a device looks up that array's
+ * address (make it before any stream capture).  Asynchronous on `stream` (a cudaStream_t; NULL
+ * is the default stream).  All calls share the array: calls that overlap on the GPU race. */
+tlbm_status tlbm_mass_static(int q, int precision, int64_t n_cells, const void* populations,
+                             double* mass, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -34,6 +34,7 @@ UNITS = [
     ("kernels_ref.cu", ["-fmad=false"]),
     ("kernels_common.cu", ["-fmad=false"]),
     ("kernels_fast.cu", []),
+    ("mass_static.cu", []),
     ("engine.cpp", ["-x", "cu"]),
     ("capi.cpp", ["-x", "cu"]),
 ]
