@@ -322,6 +322,73 @@ def run_ours(args, dist):
         out["e2e"] = e2e(args, g, p, dist)
         if dist.rank == 0 and dist.world == 1:
             out["cpu_baseline"] = cpu_baseline(g, p)
+            out["extras"] = extras(args, g, p, dist)
+    return out
+
+
+def variant_line(g, p, lattice, precision, arithmetic, steps, device):
+    """MLUPS and HBM fraction of one storage/lattice form on the same geometry."""
+    import tlbm_gb300 as T
+    from tlbm_gb300 import geometry as G
+
+    pv = G.params_lattice_units(g, lattice, p.u_lbm, 200.0, g.lo, steps, cs=p.cs, rho_lbm=1.0)
+    part = T.TLBMPartition.from_arrays(T.problem_from_params(pv), g.nd_type, precision=precision,
+                                       arithmetic=arithmetic, device=device)
+    part.run(0, 4)
+    ms = part.time_steps(4, steps)
+    part.close()
+    q = int(lattice[3:])
+    sb = {"f64": 8, "f32": 4, "bf16": 2, "f16": 2}[precision]
+    mlups = g.num_nodes * steps / (ms / 1e3) / 1e6
+    peak, _ = peaks()
+    return {"lattice": lattice, "precision": precision, "arithmetic": arithmetic,
+            "mlups": round(mlups, 1),
+            "hbm_frac": round(mlups * 1e6 * (2 * q * sb + 1) / 1e9 / peak, 4)}
+
+
+def ensemble_line(device, steps=200, seed=7):
+    """The 64-channel batched ensemble (FP32, D3Q15/D3Q19 mix): autotuned tile shape, MLUPS."""
+    import tlbm_gb300 as T
+    from tlbm_gb300 import geometry as G
+
+    chs = G.ensemble_channels(64, seed=seed, num_ts=2000)
+    ens = T.Ensemble([T.problem_from_params(pp) for _, pp in chs], [gg.nd_type for gg, _ in chs],
+                     precision="f32", device=device)
+    tiles = ens.autotune(steps=20)
+    ens.run(0, 4)
+    l0 = ens.kernel_launches()
+    ms = ens.time_steps(4, steps)
+    launches = ens.kernel_launches() - l0
+    cells = ens.cells
+    bytes_step = sum(gg.num_nodes * (2 * int(pp.lattice[3:]) * 4 + 1) for gg, pp in chs)
+    finite = all(np.isfinite(ens.mass(k)) for k in range(len(chs)))
+    ens.close()
+    peak, _ = peaks()
+    return {"channels": len(chs), "cells": cells, "steps": steps, "tiles": list(tiles),
+            "mlups": round(cells * steps / (ms / 1e3) / 1e6, 1),
+            "hbm_frac": round(bytes_step * steps / (ms / 1e3) / 1e9 / peak, 4),
+            "launches_per_step": launches / steps, "all_finite": finite}
+
+
+def extras(args, g, p, dist):
+    from tlbm_gb300 import geometry as G
+    from tlbm_gb300 import studies
+
+    out = {"lines": []}
+    for lat, prec in (("D3Q27", "f64"), ("D3Q19", "f32"), ("D3Q27", "f32"), ("D3Q19", "bf16"),
+                      ("D3Q19", "f16")):
+        out["lines"].append(variant_line(g, p, lat, prec, "fast", 50, dist.local))
+    out["lines"].append(variant_line(g, p, "D3Q19", "f64", "reference", 20, dist.local))
+    out["ensemble"] = ensemble_line(dist.local)
+    # storage-precision error after 1000 steps on a 256x128x128 pack, against the FP64
+    # reference-exact run (byte-identical to the CPU reference)
+    gs = G.random_sphere_pack(256, 128, 128, 4.0, 12.0, 0.7, seed=args.seed)
+    ps = G.params_lattice_units(gs, "D3Q19", 0.04, 200.0, gs.lo, 1000, cs=0.1, rho_lbm=1.0)
+    res = studies.precision_study(gs, ps, 1000, forms=("f64-fast", "f32", "f16", "bf16"),
+                                  device=dist.local)
+    out["precision_1000_steps_256x128x128"] = {
+        k: {kk: (round(vv, 9) if isinstance(vv, float) else vv) for kk, vv in v.items()}
+        for k, v in res.items()}
     return out
 
 

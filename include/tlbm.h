@@ -182,6 +182,37 @@ tlbm_status tlbm_mass(tlbm_handle* h, double* mass);
 /* Number of kernels this handle has launched since creation. */
 int64_t tlbm_kernel_launches(const tlbm_handle* h);
 
+/* ---- batched ensembles ---------------------------------------------------------------------
+ * No counterpart in the reference (which runs one channel per job).  `n` independent channels
+ * -- each its own tlbm_problem (lattice D3Q15 or D3Q19, size, omega, cs, inlet velocity, outlet
+ * density) and node types 0-3 -- advance together: every step is ONE persistent launch over a
+ * list of tiles covering all channels, and runs of steps replay a CUDA graph.  Each cell is
+ * computed exactly as a single-lattice handle with TLBM_ARITH_FAST computes it, so a channel's
+ * fields equal those of a tlbm_handle on the same problem bit for bit.  Storage precision from
+ * opt->precision; the arithmetic is always the fast one. */
+typedef struct tlbm_ensemble tlbm_ensemble;
+
+tlbm_status tlbm_ensemble_create(int n, const tlbm_problem* problems,
+                                 const int32_t* const* nd_types, const tlbm_options* opt,
+                                 tlbm_ensemble** out);
+tlbm_status tlbm_ensemble_destroy(tlbm_ensemble* e);
+/* Tile shape: block_x threads (multiple of 32) x block_y rows, cells_per_thread along x. */
+tlbm_status tlbm_ensemble_set_tiles(tlbm_ensemble* e, int block_x, int block_y,
+                                    int cells_per_thread);
+/* Times each candidate tile shape over `steps` steps, keeps the fastest, then returns every
+ * channel to its initial state; the chosen shape is written to the out-pointers (may be NULL). */
+tlbm_status tlbm_ensemble_autotune(tlbm_ensemble* e, int steps, int* block_x, int* block_y,
+                                   int* cells_per_thread);
+tlbm_status tlbm_ensemble_run(tlbm_ensemble* e, int first_ts, int nsteps);
+tlbm_status tlbm_ensemble_time_steps(tlbm_ensemble* e, int first_ts, int nsteps, float* ms);
+/* Macroscopic fields of one channel after the last step (global order of that channel). */
+tlbm_status tlbm_ensemble_copy_macros(tlbm_ensemble* e, int channel, void* ux, void* uy,
+                                      void* uz, void* rho);
+tlbm_status tlbm_ensemble_mass(tlbm_ensemble* e, int channel, double* mass);
+int64_t tlbm_ensemble_cells(const tlbm_ensemble* e);
+int64_t tlbm_ensemble_kernel_launches(const tlbm_ensemble* e);
+const char* tlbm_ensemble_last_error(const tlbm_ensemble* e);
+
 /* ---- allocation-free mass reduction --------------------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device memory while they
  * run -- applications that reserve the whole GPU for their own memory pool up front, or loops

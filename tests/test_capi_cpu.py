@@ -147,6 +147,21 @@ def test_null_handle_calls(lib):
     assert lib.tlbm_destroy(None) == T.ERR_INVALID_ARGUMENT
 
 
+def test_ensemble_input_validation(lib):
+    """Ensemble inputs are checked before any device work: lattice and node types."""
+    g = G.sphere_in_box(8, 8, 12, 2, 4, 4, 5)
+    p27 = G.params_lattice_units(g, "D3Q27", 0.04, 20.0, 4.0, 10)
+    with pytest.raises(T.TLBMError) as e:
+        T.Ensemble([T.problem_from_params(p27)], [g.nd_type])
+    assert e.value.status == T.ERR_UNSUPPORTED
+    p19 = G.params_lattice_units(g, "D3Q19", 0.04, 20.0, 4.0, 10)
+    nd = g.nd_type.copy()
+    nd[3] = 5
+    with pytest.raises(T.TLBMError) as e:
+        T.Ensemble([T.problem_from_params(p19)], [nd])
+    assert e.value.status == T.ERR_OUT_OF_RANGE
+
+
 def test_python_mirror_raises(lib, tmp_path):
     with pytest.raises(T.TLBMError) as e:
         T.TLBMPartition(str(tmp_path))

@@ -302,3 +302,98 @@ def run_like_tlbmexec(part: TLBMPartition) -> None:
             part.write_data()
     if part.get_time_avg_flag() == 1:
         part.write_time_avg_data()
+
+
+class Ensemble:
+    """A batch of independent channels advanced by one persistent launch per step
+    (``tlbm_ensemble_*`` in include/tlbm.h)."""
+
+    _SIG = {
+        "tlbm_ensemble_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                                ctypes.c_void_p,
+                                                ctypes.POINTER(ctypes.c_void_p)]),
+        "tlbm_ensemble_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+        "tlbm_ensemble_set_tiles": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.c_int] * 3),
+        "tlbm_ensemble_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]
+                                   + [ctypes.POINTER(ctypes.c_int)] * 3),
+        "tlbm_ensemble_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+        "tlbm_ensemble_time_steps": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                                    ctypes.POINTER(ctypes.c_float)]),
+        "tlbm_ensemble_copy_macros": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]
+                                      + [ctypes.c_void_p] * 4),
+        "tlbm_ensemble_mass": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int,
+                                              ctypes.POINTER(ctypes.c_double)]),
+        "tlbm_ensemble_cells": (ctypes.c_int64, [ctypes.c_void_p]),
+        "tlbm_ensemble_kernel_launches": (ctypes.c_int64, [ctypes.c_void_p]),
+        "tlbm_ensemble_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    }
+
+    def __init__(self, problems, nd_types, precision="f32", device=0, block_x=0, block_y=0):
+        L = library()
+        for name, (res, args) in self._SIG.items():
+            fn = getattr(L, name)
+            fn.restype, fn.argtypes = res, args
+        self._L = L
+        n = len(problems)
+        self._probs = (Problem * n)(*problems)
+        self._nd = [np.ascontiguousarray(a, dtype=np.int32) for a in nd_types]
+        ptrs = (ctypes.c_void_p * n)(*[a.ctypes.data for a in self._nd])
+        o = options(precision, "fast", block_x, block_y, device)
+        self._h = ctypes.c_void_p()
+        st = L.tlbm_ensemble_create(n, ctypes.cast(self._probs, ctypes.c_void_p),
+                                    ctypes.cast(ptrs, ctypes.c_void_p), ctypes.byref(o),
+                                    ctypes.byref(self._h))
+        if st != OK:
+            raise TLBMError(st, L.tlbm_ensemble_last_error(None).decode())
+        self.sizes = [p.nx * p.ny * p.nz for p in problems]
+        self.dtype = np.float64 if precision == "f64" else np.float32
+
+    def _check(self, st):
+        if st != OK:
+            raise TLBMError(st, self._L.tlbm_ensemble_last_error(self._h).decode())
+
+    def set_tiles(self, bx, by, cells_per_thread=1):
+        self._check(self._L.tlbm_ensemble_set_tiles(self._h, bx, by, cells_per_thread))
+
+    def autotune(self, steps=20):
+        v = [ctypes.c_int(0) for _ in range(3)]
+        self._check(self._L.tlbm_ensemble_autotune(self._h, steps, *[ctypes.byref(x) for x in v]))
+        return tuple(x.value for x in v)
+
+    def run(self, first_ts, nsteps):
+        self._check(self._L.tlbm_ensemble_run(self._h, first_ts, nsteps))
+
+    def time_steps(self, first_ts, nsteps):
+        ms = ctypes.c_float(0)
+        self._check(self._L.tlbm_ensemble_time_steps(self._h, first_ts, nsteps, ctypes.byref(ms)))
+        return ms.value
+
+    def macros(self, channel):
+        n = self.sizes[channel]
+        out = [np.empty(n, self.dtype) for _ in range(4)]
+        self._check(self._L.tlbm_ensemble_copy_macros(self._h, channel,
+                                                      *[a.ctypes.data for a in out]))
+        return out
+
+    def mass(self, channel):
+        m = ctypes.c_double(0)
+        self._check(self._L.tlbm_ensemble_mass(self._h, channel, ctypes.byref(m)))
+        return m.value
+
+    @property
+    def cells(self):
+        return self._L.tlbm_ensemble_cells(self._h)
+
+    def kernel_launches(self):
+        return self._L.tlbm_ensemble_kernel_launches(self._h)
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.tlbm_ensemble_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -35,6 +35,8 @@ UNITS = [
     ("kernels_common.cu", ["-fmad=false"]),
     ("kernels_fast.cu", []),
     ("mass_static.cu", []),
+    ("kernels_ensemble.cu", []),
+    ("ensemble.cpp", ["-x", "cu"]),
     ("engine.cpp", ["-x", "cu"]),
     ("capi.cpp", ["-x", "cu"]),
 ]

@@ -236,3 +236,102 @@ tlbm_status tlbm_mass(tlbm_handle* h, double* mass) {
 int64_t tlbm_kernel_launches(const tlbm_handle* h) { return valid(h) ? h->engine->launches() : -1; }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------- ensembles
+
+#include "ensemble.h"
+
+struct tlbm_ensemble {
+  tlbm::Ensemble* e = nullptr;
+  std::string error;
+};
+
+namespace {
+tlbm_status wrap_e(tlbm_ensemble* h, const tlbm::Status& s) {
+  if (!s.good() && h) h->error = s.msg;
+  return s.code;
+}
+bool valid_e(const tlbm_ensemble* h) { return h && h->e; }
+}  // namespace
+
+#define TLBM_ECALL(h, expr)                                                          \
+  do {                                                                               \
+    if (!valid_e(h)) return TLBM_ERR_INVALID_ARGUMENT;                               \
+    try {                                                                            \
+      return wrap_e(h, (expr));                                                      \
+    } catch (const std::bad_alloc&) {                                                \
+      return wrap_e(h, tlbm::Status::err(TLBM_ERR_NO_MEMORY, "out of host memory")); \
+    }                                                                                \
+  } while (0)
+
+extern "C" {
+
+tlbm_status tlbm_ensemble_create(int n, const tlbm_problem* problems,
+                                 const int32_t* const* nd_types, const tlbm_options* opt,
+                                 tlbm_ensemble** out) {
+  try {
+    if (!out || !problems || !nd_types || n < 1)
+      return fail_create(tlbm::Status::err(TLBM_ERR_INVALID_ARGUMENT, "bad ensemble arguments"));
+    *out = nullptr;
+    tlbm_options o;
+    tlbm_default_options(&o);
+    if (opt) {
+      if (opt->struct_size < (int)offsetof(tlbm_options, reserved) ||
+          opt->struct_size > (int)sizeof(tlbm_options))
+        return fail_create(tlbm::Status::err(TLBM_ERR_INVALID_ARGUMENT, "bad options.struct_size"));
+      std::memcpy(&o, opt, static_cast<size_t>(opt->struct_size));
+    }
+    tlbm::Ensemble* e = nullptr;
+    tlbm::Status s = tlbm::Ensemble::create(n, problems, nd_types, o, &e);
+    if (!s.good()) return fail_create(s);
+    tlbm_ensemble* h = new (std::nothrow) tlbm_ensemble();
+    if (!h) {
+      delete e;
+      return fail_create(tlbm::Status::err(TLBM_ERR_NO_MEMORY, "out of host memory"));
+    }
+    h->e = e;
+    *out = h;
+    return TLBM_OK;
+  } catch (const std::bad_alloc&) {
+    return fail_create(tlbm::Status::err(TLBM_ERR_NO_MEMORY, "out of host memory"));
+  }
+}
+
+tlbm_status tlbm_ensemble_destroy(tlbm_ensemble* h) {
+  if (!h) return TLBM_ERR_INVALID_ARGUMENT;
+  delete h->e;
+  delete h;
+  return TLBM_OK;
+}
+
+tlbm_status tlbm_ensemble_set_tiles(tlbm_ensemble* h, int bx, int by, int cpt) {
+  TLBM_ECALL(h, h->e->set_tiles(bx, by, cpt));
+}
+tlbm_status tlbm_ensemble_autotune(tlbm_ensemble* h, int steps, int* bx, int* by, int* cpt) {
+  TLBM_ECALL(h, h->e->autotune(steps, bx, by, cpt));
+}
+tlbm_status tlbm_ensemble_run(tlbm_ensemble* h, int first_ts, int nsteps) {
+  TLBM_ECALL(h, h->e->run(first_ts, nsteps));
+}
+tlbm_status tlbm_ensemble_time_steps(tlbm_ensemble* h, int first_ts, int nsteps, float* ms) {
+  if (!ms) return TLBM_ERR_INVALID_ARGUMENT;
+  TLBM_ECALL(h, h->e->time_steps(first_ts, nsteps, ms));
+}
+tlbm_status tlbm_ensemble_copy_macros(tlbm_ensemble* h, int channel, void* ux, void* uy, void* uz,
+                                      void* rho) {
+  TLBM_ECALL(h, h->e->copy_macros(channel, ux, uy, uz, rho));
+}
+tlbm_status tlbm_ensemble_mass(tlbm_ensemble* h, int channel, double* mass) {
+  if (!mass) return TLBM_ERR_INVALID_ARGUMENT;
+  TLBM_ECALL(h, h->e->mass(channel, mass));
+}
+int64_t tlbm_ensemble_cells(const tlbm_ensemble* h) { return valid_e(h) ? h->e->cells() : -1; }
+int64_t tlbm_ensemble_kernel_launches(const tlbm_ensemble* h) {
+  return valid_e(h) ? h->e->launches() : -1;
+}
+const char* tlbm_ensemble_last_error(const tlbm_ensemble* h) {
+  if (!h) return g_create_error.c_str();
+  return h->error.c_str();
+}
+
+}  // extern "C"

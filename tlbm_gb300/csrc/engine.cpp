@@ -387,11 +387,13 @@ Status Engine::init(const int32_t* nd_type, const int32_t* parts, int size) {
   pb_.n = n_;
   pb_.nd_type = d_type_;
   pb_.omega = prob_.omega;
+  pb_.nu = (1.0 / prob_.omega - 0.5) / 3.0;
   pb_.cs = prob_.cs;
   pb_.u_bc = prob_.u_lbm;
   pb_.rho_bc = prob_.rho_lbm;
   pb_.dynamics = prob_.dynamics;
   pb_.has_type5 = has_type5_ ? 1 : 0;
+  fill_derived(pb_, q_, sb_);
 
   const int nb = mass_blocks(pb_);
   TLBM_CUDA(cudaMalloc(&d_partial_, nb * sizeof(double)));

@@ -19,9 +19,58 @@ struct DevProblem {
   int64_t n;       // nx*ny*nz (< 2^31 so cell offsets fit in int)
   const uint8_t* nd_type;
   double omega, cs, u_bc, rho_bc;  // the parsed `real` values, held exactly
+  double nu;                        // (1/omega - 1/2)/3, the molecular viscosity
+  // the same values rounded to float once on the host (a float kernel converting doubles per
+  // thread would spend FP64-pipe slots on it)
+  float omega_f, cs_f, u_bc_f, rho_bc_f, nu_f;
   int dynamics;
   int has_type5;
+  // byte offset, from a cell's own population of speed 0, of the population of speed i that an
+  // interior cell (no face of the box) pulls: i*n*bytes - (ex + ey*nx + ez*nx*ny)*bytes
+  long long pull_off[27];
 };
+
+// problem parameters in the compute type
+template <class C>
+struct Par;
+template <>
+struct Par<double> {
+  static TLBM_HD double omega(const DevProblem& p) { return p.omega; }
+  static TLBM_HD double cs(const DevProblem& p) { return p.cs; }
+  static TLBM_HD double u_bc(const DevProblem& p) { return p.u_bc; }
+  static TLBM_HD double rho_bc(const DevProblem& p) { return p.rho_bc; }
+  static TLBM_HD double nu(const DevProblem& p) { return p.nu; }
+};
+template <>
+struct Par<float> {
+  static TLBM_HD float omega(const DevProblem& p) { return p.omega_f; }
+  static TLBM_HD float cs(const DevProblem& p) { return p.cs_f; }
+  static TLBM_HD float u_bc(const DevProblem& p) { return p.u_bc_f; }
+  static TLBM_HD float rho_bc(const DevProblem& p) { return p.rho_bc_f; }
+  static TLBM_HD float nu(const DevProblem& p) { return p.nu_f; }
+};
+
+// fills the float copies and the interior pull offsets of `pb` for q speeds of `bytes` each
+template <class L>
+inline void fill_pull_offsets(DevProblem& pb, int bytes) {
+  for (int i = 0; i < 27; ++i) pb.pull_off[i] = 0;
+  for (int i = 0; i < L::Q; ++i)
+    pb.pull_off[i] = (static_cast<long long>(i) * pb.n -
+                      (L::ex(i) + static_cast<long long>(L::ey(i)) * pb.nx +
+                       static_cast<long long>(L::ez(i)) * pb.nxy)) *
+                     bytes;
+}
+
+inline void fill_derived(DevProblem& pb, int q, int bytes) {
+  pb.omega_f = static_cast<float>(pb.omega);
+  pb.cs_f = static_cast<float>(pb.cs);
+  pb.u_bc_f = static_cast<float>(pb.u_bc);
+  pb.rho_bc_f = static_cast<float>(pb.rho_bc);
+  pb.nu_f = static_cast<float>(pb.nu);
+  if (q == 15) fill_pull_offsets<Lattice<15>>(pb, bytes);
+  if (q == 19) fill_pull_offsets<Lattice<19>>(pb, bytes);
+  if (q == 27) fill_pull_offsets<Lattice<27>>(pb, bytes);
+}
 
 // offsets of a cell and its periodic neighbours along each axis
 struct Nbr {

@@ -5,113 +5,18 @@
 // storage.cuh.  Solid nodes move the raw stored values (bounce-back needs no arithmetic, and
 // opposite speeds share a weight, so the f - w shift of 16-bit storage carries over unchanged).
 #include "kernels.h"
-#include "physics_fast.cuh"
-#include "storage.cuh"
+#include "step_fast.cuh"
 
 namespace tlbm {
 namespace {
 
-template <class L, int K>
-__device__ __forceinline__ void load_cell(const typename Store<K>::T* __restrict__ src, size_t n,
-                                          const Nbr& nb, typename Store<K>::T (&raw)[L::Q]) {
-#pragma unroll
-  for (int i = 0; i < L::Q; ++i) raw[i] = __ldg(src + i * n + nb.from<L>(i));
-}
-
-template <class L, int K>
-__device__ __forceinline__ void unpack(const typename Store<K>::T (&raw)[L::Q],
-                                       typename Store<K>::C (&f)[L::Q]) {
-  using S = Store<K>;
-  using C = typename S::C;
-#pragma unroll
-  for (int i = 0; i < L::Q; ++i) f[i] = S::load(raw[i], fast::wgt<L, C>(i));
-}
-
-// node macroscopic values as the reference holds them after processing the node
-template <class L, class C>
-__device__ __forceinline__ void node_macros(uint8_t t, const C (&f)[L::Q], C u_bc, C rho_bc,
-                                            C& rho, C& ux, C& uy, C& uz) {
-  if (t == kSolid) {
-    rho = fast::density<L, C>(f);
-    ux = uy = uz = C(0);
-  } else if (t == kInlet) {
-    rho = fast::inlet_rho<L, C>(f, C(1) / (C(1) - u_bc));
-    ux = uy = C(0);
-    uz = u_bc;
-  } else {
-    fast::moments<L, C>(f, rho, ux, uy, uz);
-    if (t == kOutlet) {
-      rho = rho_bc;
-      uz = fast::outlet_uz<L, C>(f, C(1) / rho_bc);
-    }
-  }
-}
-
 template <class L, int K, bool kSmag>
 __global__ void __launch_bounds__(128) k_step_fast(StepArgs a) {
-  using S = Store<K>;
-  using C = typename S::C;
-  using T = typename S::T;
-  const DevProblem& pb = a.pb;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
-  if (x >= pb.nx || y >= pb.ny) return;
-  const Nbr nb(x, y, z, pb.nx, pb.ny, pb.nz, pb.nxy);
-  const int c = nb.self();
-  const size_t n = static_cast<size_t>(pb.n);
-  const T* __restrict__ src = static_cast<const T*>(a.src);
-  T* __restrict__ dst = static_cast<T*>(a.dst);
-
-  T raw[L::Q];
-  load_cell<L, K>(src, n, nb, raw);
-  const uint8_t t = pb.nd_type[c];
-  C rho = 0, ux = 0, uy = 0, uz = 0;
-  if (t == kSolid) {
-#pragma unroll
-    for (int i = 0; i < L::Q; ++i) dst[i * n + c] = raw[L::bb(i)];
-    if (a.time_avg) {
-      C f[L::Q];
-      unpack<L, K>(raw, f);
-      rho = fast::density<L, C>(f);
-    }
-  } else {
-    C f[L::Q];
-    unpack<L, K>(raw, f);
-    const C u_bc = static_cast<C>(pb.u_bc);
-    node_macros<L, C>(t, f, u_bc, static_cast<C>(pb.rho_bc), rho, ux, uy, uz);
-    if (pb.has_type5 && t == kMovingWall) {
-      const C* cur = static_cast<const C*>(a.uyq_cur);
-      const C* prev = static_cast<const C*>(a.uyq_prev);
-#pragma unroll
-      for (int i = 0; i < L::Q; ++i) {
-        const C uyq = i <= c ? cur[i] : prev[i];
-        f[i] += C(3) * rho * fast::wgt<L, C>(i) *
-                (C(L::ez(i)) * (u_bc - uz) - C(L::ex(i)) * ux - C(L::ey(i)) * uyq);
-      }
-    }
-    C feq[L::Q];
-    fast::equilibrium<L, C>(rho, ux, uy, uz, feq);
-    if (t == kInlet) fast::nebb<L, C, true>(f, feq);
-    if (t == kOutlet) fast::nebb<L, C, false>(f, feq);
-    if (pb.dynamics == 1) {
-      C om = static_cast<C>(pb.omega);
-      if constexpr (kSmag) {
-        const C nu = (C(1) / om - C(0.5)) / C(3);
-        om = fast::smagorinsky_omega<L, C>(f, feq, static_cast<C>(pb.cs), nu);
-      }
-      fast::relax<L, C>(f, feq, om);
-    }
-#pragma unroll
-    for (int i = 0; i < L::Q; ++i) dst[i * n + c] = S::save(f[i], fast::wgt<L, C>(i));
-  }
-  if (a.time_avg) {
-    C* const* avg = reinterpret_cast<C* const*>(a.avg);
-    avg[0][c] += ux;
-    avg[1][c] += uy;
-    avg[2][c] += uz;
-    avg[3][c] += rho;
-  }
+  if (x >= a.pb.nx || y >= a.pb.ny) return;
+  cell_step<L, K, kSmag>(a, x, y, z);
 }
 
 template <class L, int K>

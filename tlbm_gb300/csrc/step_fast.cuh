@@ -1,0 +1,146 @@
+// step_fast.cuh -- one cell of the fused stream-collide step in fast arithmetic.
+//
+// Shared by the single-lattice kernel (kernels_fast.cu) and the batched-ensemble kernel
+// (kernels_ensemble.cu), so both compute every cell with the same instructions.  The cell
+// pulls its Q populations from c - e_i (periodic), branches on its node type, collides in
+// registers and stores at c:
+//   fluid        -> pair-form BGK / Smagorinsky (physics_fast.cuh: fluid_collide)
+//   solid        -> bounce-back of the raw stored values, no collision
+//   inlet/outlet -> the reference's density/velocity rule, non-equilibrium bounce-back of the
+//                   unknown speeds, then BGK / Smagorinsky
+//   moving wall  -> the reference's set_uz_bc nudge (uy of node number i, see physics_ref.cuh)
+#pragma once
+
+#include "kernels.h"
+#include "physics_fast.cuh"
+#include "storage.cuh"
+
+namespace tlbm {
+
+template <class L, int K>
+__device__ __forceinline__ void load_cell(const typename Store<K>::T* __restrict__ src, size_t n,
+                                          const Nbr& nb, typename Store<K>::T (&raw)[L::Q]) {
+#pragma unroll
+  for (int i = 0; i < L::Q; ++i) raw[i] = __ldg(src + i * n + nb.from<L>(i));
+}
+
+template <class L, int K>
+__device__ __forceinline__ void unpack(const typename Store<K>::T (&raw)[L::Q],
+                                       typename Store<K>::C (&f)[L::Q]) {
+  using S = Store<K>;
+  using C = typename S::C;
+#pragma unroll
+  for (int i = 0; i < L::Q; ++i) f[i] = S::load(raw[i], fast::wgt<L, C>(i));
+}
+
+// node macroscopic values as the reference holds them after processing the node
+template <class L, class C>
+__device__ __forceinline__ void node_macros(uint8_t t, const C (&f)[L::Q], C u_bc, C rho_bc,
+                                            C& rho, C& ux, C& uy, C& uz) {
+  if (t == kSolid) {
+    rho = fast::density<L, C>(f);
+    ux = uy = uz = C(0);
+  } else if (t == kInlet) {
+    rho = fast::inlet_rho<L, C>(f, C(1) / (C(1) - u_bc));
+    ux = uy = C(0);
+    uz = u_bc;
+  } else {
+    fast::moments<L, C>(f, rho, ux, uy, uz);
+    if (t == kOutlet) {
+      rho = rho_bc;
+      uz = fast::outlet_uz<L, C>(f, C(1) / rho_bc);
+    }
+  }
+}
+
+template <class L, int K, bool kSmag>
+__device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z) {
+  using S = Store<K>;
+  using C = typename S::C;
+  using T = typename S::T;
+  const DevProblem& pb = a.pb;
+  const int c = x + y * pb.nx + z * pb.nxy;
+  const size_t n = static_cast<size_t>(pb.n);
+  const T* __restrict__ src = static_cast<const T*>(a.src);
+  T* __restrict__ dst = static_cast<T*>(a.dst);
+
+  T raw[L::Q];
+  if (x > 0 && x < pb.nx - 1 && y > 0 && y < pb.ny - 1 && z > 0 && z < pb.nz - 1) {
+    // interior cell: speed i comes from a fixed byte offset of the cell's own slot
+    const char* base = reinterpret_cast<const char*>(src + c);
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i)
+      raw[i] = __ldg(reinterpret_cast<const T*>(base + pb.pull_off[i]));
+  } else {
+    const Nbr nb(x, y, z, pb.nx, pb.ny, pb.nz, pb.nxy);
+    load_cell<L, K>(src, n, nb, raw);
+  }
+  const uint8_t t = pb.nd_type[c];
+  C rho = 0, ux = 0, uy = 0, uz = 0;
+  if (t == kFluid) {
+    C f[L::Q];
+    unpack<L, K>(raw, f);
+    fast::fluid_collide<L, C, kSmag>(f, Par<C>::omega(pb), Par<C>::cs(pb), Par<C>::nu(pb),
+                                     pb.dynamics == 1, rho, ux, uy, uz);
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) dst[i * n + c] = S::save(f[i], fast::wgt<L, C>(i));
+  } else if (t == kSolid) {
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) dst[i * n + c] = raw[L::bb(i)];
+    if (a.time_avg) {
+      C f[L::Q];
+      unpack<L, K>(raw, f);
+      rho = fast::density<L, C>(f);
+    }
+  } else {
+    C f[L::Q];
+    unpack<L, K>(raw, f);
+    const C u_bc = Par<C>::u_bc(pb);
+    node_macros<L, C>(t, f, u_bc, Par<C>::rho_bc(pb), rho, ux, uy, uz);
+    if constexpr (S::kShifted) {
+      // 16-bit storage: the inlet density and outlet velocity sums are taken in FP64
+      if (t == kInlet || t == kOutlet) {
+        double fd[L::Q];
+#pragma unroll
+        for (int i = 0; i < L::Q; ++i)
+          fd[i] = static_cast<double>(fast::wgt<L, float>(i)) +
+                  static_cast<double>(S::load(raw[i], 0.0f));
+        if (t == kInlet)
+          rho = static_cast<C>(fast::inlet_rho<L, double>(fd, 1.0 / (1.0 - pb.u_bc)));
+        else
+          uz = static_cast<C>(fast::outlet_uz<L, double>(fd, 1.0 / pb.rho_bc));
+      }
+    }
+    if (pb.has_type5 && t == kMovingWall) {
+      const C* cur = static_cast<const C*>(a.uyq_cur);
+      const C* prev = static_cast<const C*>(a.uyq_prev);
+#pragma unroll
+      for (int i = 0; i < L::Q; ++i) {
+        const C uyq = i <= c ? cur[i] : prev[i];
+        f[i] += C(3) * rho * fast::wgt<L, C>(i) *
+                (C(L::ez(i)) * (u_bc - uz) - C(L::ex(i)) * ux - C(L::ey(i)) * uyq);
+      }
+    }
+    C feq[L::Q];
+    fast::equilibrium<L, C>(rho, ux, uy, uz, feq);
+    if (t == kInlet) fast::nebb<L, C, true>(f, feq);
+    if (t == kOutlet) fast::nebb<L, C, false>(f, feq);
+    if (pb.dynamics == 1) {
+      C om = Par<C>::omega(pb);
+      if constexpr (kSmag)
+        om = fast::smagorinsky_omega<L, C>(f, feq, Par<C>::cs(pb), Par<C>::nu(pb));
+      fast::relax<L, C>(f, feq, om);
+    }
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) dst[i * n + c] = S::save(f[i], fast::wgt<L, C>(i));
+  }
+  if (a.time_avg) {
+    C* const* avg = reinterpret_cast<C* const*>(a.avg);
+    avg[0][c] += ux;
+    avg[1][c] += uy;
+    avg[2][c] += uz;
+    avg[3][c] += rho;
+  }
+}
+
+}  // namespace tlbm
