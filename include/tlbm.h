@@ -182,6 +182,46 @@ tlbm_status tlbm_mass(tlbm_handle* h, double* mass);
 /* Number of kernels this handle has launched since creation. */
 int64_t tlbm_kernel_launches(const tlbm_handle* h);
 
+/* ---- inflow, learned closure, filtering --------------------------------------------------
+ * No counterpart in the reference (its inlet velocity is the scalar uLBM,
+ * src/TLBM_Partition.cpp:765-766, and its only closure is Smagorinsky).  Fast arithmetic only. */
+
+/* Inlet velocity u_z per (x, y) of the z = 0 plane: nx*ny values in order x + y*nx (NULL
+ * restores the uniform uLBM).  Used for seeded inlet perturbations. */
+tlbm_status tlbm_set_inlet_profile(tlbm_handle* h, const double* uz);
+
+/* Learned eddy-viscosity closure for fluid nodes: an 8-32-32-1 tanh MLP (1377 FP32 parameters:
+ * W1[32][8], b1[32], W2[32][32], b2[32], w3[32], b3; weights run in BF16) on the normalised
+ * features (raw_k - shift[k]) * scale[k] of raw = [Pi_xx, Pi_yy, Pi_zz, Pi_xy, Pi_xz, Pi_yz,
+ * rho - 1, |Pi|] (Pi = non-equilibrium stress); nu_t = out_scale * y and
+ * tau = max(3 (nu + nu_t) + 1/2, tau_min), tau_min > 1/2.  A non-finite output falls back to
+ * Smagorinsky (cs from params.lbm; plain BGK when cs = 0), which inlet/outlet nodes use too.
+ * params = NULL removes the closure. */
+tlbm_status tlbm_set_closure_mlp(tlbm_handle* h, const float* params, const float* scale,
+                                 const float* shift, float out_scale, float tau_min);
+
+/* Box filter of width `factor` (dividing nx, ny, nz) of the last step's macroscopic fields:
+ * writes 10 consecutive coarse fields (rho, ux, uy, uz, ux*ux, uy*uy, uz*uz, ux*uy, ux*uz,
+ * uy*uz box means), each (nx/f)*(ny/f)*(nz/f) values of tlbm_output_bytes(h) bytes. */
+tlbm_status tlbm_filtered_fields(tlbm_handle* h, int factor, void* out);
+
+/* Training set and optimiser of the learned closure (on the GPU).  Features: n x 8 floats,
+ * already normalised; targets: n floats (normalised nu_t).  Loss: mean of (y - t)^2 / 2. */
+typedef struct tlbm_mlp tlbm_mlp;
+int tlbm_mlp_num_params(void);
+tlbm_status tlbm_mlp_create(int64_t n, const float* features, const float* targets,
+                            uint64_t seed, int device, tlbm_mlp** out);
+tlbm_status tlbm_mlp_destroy(tlbm_mlp* m);
+tlbm_status tlbm_mlp_set_params(tlbm_mlp* m, const float* params);
+tlbm_status tlbm_mlp_get_params(tlbm_mlp* m, float* params);
+/* mean loss and its gradient over samples [first, first+count) in the order given */
+tlbm_status tlbm_mlp_loss_grad(tlbm_mlp* m, int64_t first, int64_t count, float* loss,
+                               float* grad);
+/* Adam (lr; beta 0.9, 0.999) over minibatches of a seeded shuffle; epoch_loss may be NULL */
+tlbm_status tlbm_mlp_train(tlbm_mlp* m, int epochs, int64_t batch, float lr, float* epoch_loss);
+tlbm_status tlbm_mlp_predict(tlbm_mlp* m, int64_t n, const float* features, float* y);
+const char* tlbm_mlp_last_error(const tlbm_mlp* m);
+
 /* ---- batched ensembles ---------------------------------------------------------------------
  * No counterpart in the reference (which runs one channel per job).  `n` independent channels
  * -- each its own tlbm_problem (lattice D3Q15 or D3Q19, size, omega, cs, inlet velocity, outlet

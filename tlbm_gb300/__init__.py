@@ -107,6 +107,18 @@ def library(path: str = LIB_PATH):
         "tlbm_copy_adjacency": (i32, [H, vp]),
         "tlbm_mass": (i32, [H, ctypes.POINTER(ctypes.c_double)]),
         "tlbm_kernel_launches": (i64, [H]),
+        "tlbm_set_inlet_profile": (i32, [H, vp]),
+        "tlbm_set_closure_mlp": (i32, [H, vp, vp, vp, ctypes.c_float, ctypes.c_float]),
+        "tlbm_filtered_fields": (i32, [H, i32, vp]),
+        "tlbm_mlp_num_params": (i32, []),
+        "tlbm_mlp_create": (i32, [i64, vp, vp, ctypes.c_uint64, i32, PH]),
+        "tlbm_mlp_destroy": (i32, [H]),
+        "tlbm_mlp_set_params": (i32, [H, vp]),
+        "tlbm_mlp_get_params": (i32, [H, vp]),
+        "tlbm_mlp_loss_grad": (i32, [H, i64, i64, ctypes.POINTER(ctypes.c_float), vp]),
+        "tlbm_mlp_train": (i32, [H, i32, i64, ctypes.c_float, vp]),
+        "tlbm_mlp_predict": (i32, [H, i64, vp, vp]),
+        "tlbm_mlp_last_error": (ctypes.c_char_p, [H]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -159,6 +171,11 @@ class TLBMPartition:
             o = options(precision or "f32", arithmetic, block_x, block_y, device)
             _check(self._L.tlbm_create_ex(workdir.encode(), rank, size, ctypes.byref(o),
                                           ctypes.byref(self._h)))
+        try:
+            toks = open(os.path.join(workdir, "params.lbm")).read().split()
+            self._dims = (int(toks[10]), int(toks[11]), int(toks[12]))
+        except (OSError, IndexError, ValueError):
+            pass
         self._init_meta()
 
     @classmethod
@@ -177,6 +194,7 @@ class TLBMPartition:
         obj._L = L
         obj._h = h
         obj.workdir = workdir
+        obj._dims = (problem.nx, problem.ny, problem.nz)
         obj._init_meta()
         return obj
 
@@ -258,6 +276,42 @@ class TLBMPartition:
 
     def kernel_launches(self) -> int:
         return self._L.tlbm_kernel_launches(self._h)
+
+    def set_inlet_profile(self, uz) -> None:
+        """Inlet u_z per (x, y) of the z = 0 plane (None restores the uniform uLBM)."""
+        if uz is None:
+            _check(self._L.tlbm_set_inlet_profile(self._h, None), self._h)
+            return
+        self._inlet = np.ascontiguousarray(uz, dtype=np.float64).reshape(-1)
+        _check(self._L.tlbm_set_inlet_profile(self._h, self._inlet.ctypes.data), self._h)
+
+    def set_closure_mlp(self, params, scale, shift, out_scale: float, tau_min: float) -> None:
+        """Install the learned eddy-viscosity closure (None removes it)."""
+        if params is None:
+            _check(self._L.tlbm_set_closure_mlp(self._h, None, None, None, 0.0, 0.0), self._h)
+            return
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        s = np.ascontiguousarray(scale, dtype=np.float32)
+        h = np.ascontiguousarray(shift, dtype=np.float32)
+        _check(self._L.tlbm_set_closure_mlp(self._h, p.ctypes.data, s.ctypes.data, h.ctypes.data,
+                                            float(out_scale), float(tau_min)), self._h)
+
+    FILTERED = ("rho", "ux", "uy", "uz", "uxux", "uyuy", "uzuz", "uxuy", "uxuz", "uyuz")
+
+    def filtered_fields(self, factor: int) -> dict:
+        """Box-filtered (width `factor`) fields of the last step, as coarse (z, y, x) arrays."""
+        p = self._shape()
+        nc = (p[0] // factor) * (p[1] // factor) * (p[2] // factor)
+        out = np.empty(10 * nc, self.dtype)
+        _check(self._L.tlbm_filtered_fields(self._h, factor, out.ctypes.data), self._h)
+        cz, cy, cx = p[2] // factor, p[1] // factor, p[0] // factor
+        return {k: out[i * nc:(i + 1) * nc].reshape(cz, cy, cx)
+                for i, k in enumerate(self.FILTERED)}
+
+    def _shape(self):
+        if not hasattr(self, "_dims"):
+            raise TLBMError(ERR_INVALID_ARGUMENT, "lattice dimensions unknown for this handle")
+        return self._dims
 
     def close(self) -> None:
         if getattr(self, "_h", None) and self._h.value:
@@ -390,6 +444,66 @@ class Ensemble:
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
             self._L.tlbm_ensemble_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class MlpTrainer:
+    """GPU training set and Adam optimiser of the learned closure (``tlbm_mlp_*``)."""
+
+    def __init__(self, features, targets, seed: int = 0, device: int = 0):
+        L = library()
+        self._L = L
+        self.n_params = L.tlbm_mlp_num_params()
+        self._x = np.ascontiguousarray(features, dtype=np.float32).reshape(-1, 8)
+        self._t = np.ascontiguousarray(targets, dtype=np.float32).reshape(-1)
+        self.n = len(self._t)
+        self._h = ctypes.c_void_p()
+        st = L.tlbm_mlp_create(self.n, self._x.ctypes.data, self._t.ctypes.data, seed, device,
+                               ctypes.byref(self._h))
+        if st != OK:
+            raise TLBMError(st, L.tlbm_mlp_last_error(None).decode())
+
+    def _check(self, st):
+        if st != OK:
+            raise TLBMError(st, self._L.tlbm_mlp_last_error(self._h).decode())
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        self._check(self._L.tlbm_mlp_set_params(self._h, p.ctypes.data))
+
+    def params(self):
+        p = np.empty(self.n_params, np.float32)
+        self._check(self._L.tlbm_mlp_get_params(self._h, p.ctypes.data))
+        return p
+
+    def loss_grad(self, first: int = 0, count: int | None = None):
+        count = self.n - first if count is None else count
+        loss = ctypes.c_float(0)
+        g = np.empty(self.n_params, np.float32)
+        self._check(self._L.tlbm_mlp_loss_grad(self._h, first, count, ctypes.byref(loss),
+                                               g.ctypes.data))
+        return loss.value, g
+
+    def train(self, epochs: int, batch: int, lr: float):
+        losses = np.empty(epochs, np.float32)
+        self._check(self._L.tlbm_mlp_train(self._h, epochs, batch, lr, losses.ctypes.data))
+        return losses
+
+    def predict(self, features):
+        x = np.ascontiguousarray(features, dtype=np.float32).reshape(-1, 8)
+        y = np.empty(len(x), np.float32)
+        self._check(self._L.tlbm_mlp_predict(self._h, len(x), x.ctypes.data, y.ctypes.data))
+        return y
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.tlbm_mlp_destroy(self._h)
             self._h = ctypes.c_void_p()
 
     def __del__(self):

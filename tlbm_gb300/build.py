@@ -37,6 +37,9 @@ UNITS = [
     ("mass_static.cu", []),
     ("kernels_ensemble.cu", []),
     ("ensemble.cpp", ["-x", "cu"]),
+    ("kernels_mlp.cu", []),
+    ("mlp_trainer.cpp", ["-x", "cu"]),
+    ("capi_mlp.cpp", ["-x", "cu"]),
     ("engine.cpp", ["-x", "cu"]),
     ("capi.cpp", ["-x", "cu"]),
 ]

@@ -1,0 +1,230 @@
+"""Learned eddy-viscosity closure: training data from the solver's own fine-grid runs, GPU
+training, and evaluation against Smagorinsky on the box-filtered fine solution.
+
+Pipeline (all on the GPU except numpy bookkeeping on coarse-sized arrays):
+
+1. A fine run (factor `f` finer in space and time, plain BGK) with a seeded, smooth inlet
+   perturbation; snapshots of its macroscopic fields are box-filtered on the device
+   (``tlbm_filtered_fields``) to the coarse grid: rho, u and the means of u_a u_b.
+2. Per coarse cell the least-squares eddy viscosity that makes the Boussinesq model reproduce
+   the filtered sub-grid stress:  nu_t* = -(tau_sgs^dev : S) / (2 S : S),
+   tau_sgs_ab = mean(u_a u_b) - mean(u_a) mean(u_b), S the strain rate of the filtered velocity
+   (central differences, periodic in x/y).  Clipped to [0, nu_cap].
+3. Features are what a coarse LBM node sees when it relaxes with tau* = 3 (nu + nu_t*) + 1/2:
+   its non-equilibrium stress Pi_ab = -2 rho c_s^2 tau* S_ab (first-order Chapman-Enskog),
+   rho - 1 and |Pi| -- the same quantities the fused collide kernel computes from f - feq.
+4. The 8-32-32-1 network is trained on the GPU (``tlbm_mlp_*``: BF16 weights, FP32
+   accumulation, Adam) and installed with ``tlbm_set_closure_mlp``.
+5. Coarse runs with Smagorinsky (cs = 0.1) and with the learned closure are compared with the
+   filtered fine run on the mean streamwise-velocity profile and on the 2-D energy spectrum of
+   u_z in x-y planes.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+from . import MlpTrainer, TLBMPartition, problem_from_params
+from . import geometry as G
+
+CS2 = 1.0 / 3.0
+
+
+# ----------------------------------------------------------------------------- flow setup
+
+
+def inlet_noise(nx: int, ny: int, factor: int = 1, modes: int = 24, seed: int = 11,
+                kmax: int = 6) -> np.ndarray:
+    """Smooth, periodic, zero-mean, unit-std perturbation on an (ny, nx) inlet plane, evaluated
+    at cell centres of a grid `factor` times finer than (nx, ny) coarse cells, so the fine and
+    coarse inlets carry the same field (the fine one box-filters to the coarse one up to the
+    sub-cell variation)."""
+    rng = np.random.default_rng(seed)
+    fx, fy = nx * factor, ny * factor
+    x = (np.arange(fx) + 0.5) / fx
+    y = (np.arange(fy) + 0.5) / fy
+    X, Y = np.meshgrid(x, y)
+    out = np.zeros((fy, fx))
+    for _ in range(modes):
+        m = int(rng.integers(-kmax, kmax + 1))
+        n = int(rng.integers(1, kmax + 1))
+        out += rng.normal() * np.sin(2 * np.pi * (m * X + n * Y) + rng.uniform(0, 2 * np.pi))
+    out -= out.mean()
+    return out / out.std()
+
+
+def channel(nx, ny, nz, u_in, re, length, lattice="D3Q19", cs=0.0, steps=1000):
+    """Periodic-x/y box with a z==0 inlet and z==nz-1 outlet (no obstacle)."""
+    nd = np.zeros((nz, ny, nx), np.int32)
+    nd[0] = G.INLET
+    nd[nz - 1] = G.OUTLET
+    g = G.Geometry(nx, ny, nz, nd.reshape(-1))
+    p = G.params_lattice_units(g, lattice, u_in, re, length, steps, cs=cs, rho_lbm=1.0)
+    return g, p
+
+
+# ----------------------------------------------------------------------------- targets / features
+
+
+def strain(ux, uy, uz):
+    """S_ab of a (z, y, x) velocity field: central differences, periodic in x and y,
+    one-sided at the z ends.  Returns (xx, yy, zz, xy, xz, yz)."""
+
+    def d(a, axis):
+        if axis in (1, 2):
+            return 0.5 * (np.roll(a, -1, axis) - np.roll(a, 1, axis))
+        return np.gradient(a, axis=0)
+
+    dux = [d(ux, 2), d(ux, 1), d(ux, 0)]
+    duy = [d(uy, 2), d(uy, 1), d(uy, 0)]
+    duz = [d(uz, 2), d(uz, 1), d(uz, 0)]
+    return (dux[0], duy[1], duz[2], 0.5 * (dux[1] + duy[0]), 0.5 * (dux[2] + duz[0]),
+            0.5 * (duy[2] + duz[1]))
+
+
+def sgs_eddy_viscosity(F: dict, nu_cap: float):
+    u = [F["ux"].astype(np.float64), F["uy"].astype(np.float64), F["uz"].astype(np.float64)]
+    S = strain(*u)
+    t = [F["uxux"] - u[0] * u[0], F["uyuy"] - u[1] * u[1], F["uzuz"] - u[2] * u[2],
+         F["uxuy"] - u[0] * u[1], F["uxuz"] - u[0] * u[2], F["uyuz"] - u[1] * u[2]]
+    tr = (t[0] + t[1] + t[2]) / 3.0
+    td = [t[0] - tr, t[1] - tr, t[2] - tr, t[3], t[4], t[5]]
+    w = [1, 1, 1, 2, 2, 2]
+    num = -sum(wk * a * b for wk, a, b in zip(w, td, S))
+    den = 2.0 * sum(wk * b * b for wk, b in zip(w, S))
+    nut = np.where(den > 1e-30, num / np.maximum(den, 1e-30), 0.0)
+    return np.clip(nut, 0.0, nu_cap), S
+
+
+def raw_features(F: dict, S, nu: float, nu_t):
+    rho = F["rho"].astype(np.float64)
+    tau = 3.0 * (nu + nu_t) + 0.5
+    pi = [-2.0 * rho * CS2 * tau * s for s in S]
+    q2 = pi[0] ** 2 + pi[1] ** 2 + pi[2] ** 2 + 2 * (pi[3] ** 2 + pi[4] ** 2 + pi[5] ** 2)
+    return np.stack(pi + [rho - 1.0, np.sqrt(q2)], axis=-1).reshape(-1, 8)
+
+
+# ----------------------------------------------------------------------------- evaluation
+
+
+def mean_profile(uz, nd):
+    """Mean u_z over each x-y plane (fluid and inlet/outlet nodes)."""
+    return uz.reshape(nd.shape).mean(axis=(1, 2))
+
+
+def spectrum(uz, z_planes):
+    """Radially binned 2-D energy spectrum of u_z fluctuations, averaged over z planes."""
+    nz, ny, nx = uz.shape
+    kx = np.fft.fftfreq(nx) * nx
+    ky = np.fft.fftfreq(ny) * ny
+    K = np.sqrt(kx[None, :] ** 2 + ky[:, None] ** 2)
+    kb = np.rint(K).astype(int)
+    nk = int(min(nx, ny) // 2)
+    e = np.zeros(nk + 1)
+    for z in z_planes:
+        a = uz[z] - uz[z].mean()
+        p = np.abs(np.fft.fft2(a)) ** 2 / (nx * ny) ** 2
+        e += np.bincount(kb.reshape(-1), p.reshape(-1), minlength=kb.max() + 1)[:nk + 1]
+    return e / len(z_planes)
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+# ----------------------------------------------------------------------------- study
+
+
+def run_fine(cx, cy, cz, factor, u_in, re, noise_amp, coarse_steps, snap_every, precision="f32",
+             device=0, seed=11):
+    """Fine BGK run; returns filtered snapshots keyed by coarse step."""
+    g, p = channel(cx * factor, cy * factor, cz * factor, u_in, re, cy * factor)
+    part = TLBMPartition.from_arrays(problem_from_params(p), g.nd_type, precision=precision,
+                                     arithmetic="fast", device=device)
+    xi = inlet_noise(cx, cy, factor, seed=seed)
+    part.set_inlet_profile(u_in * (1.0 + noise_amp * xi))
+    snaps = {}
+    ts = 0
+    for k in range(snap_every, coarse_steps + 1, snap_every):
+        part.run(ts, factor * k - ts)
+        ts = factor * k
+        snaps[k] = part.filtered_fields(factor)
+    part.close()
+    return snaps, p.omega
+
+
+def build_dataset(snaps, nu_c, nu_cap):
+    feats, targets = [], []
+    for F in snaps.values():
+        nut, S = sgs_eddy_viscosity(F, nu_cap)
+        feats.append(raw_features(F, S, nu_c, nut))
+        targets.append(nut.reshape(-1))
+    return np.concatenate(feats), np.concatenate(targets)
+
+
+def normalise(raw, targets):
+    shift = raw.mean(axis=0)
+    scale = 1.0 / np.maximum(raw.std(axis=0), 1e-30)
+    out_scale = max(float(targets.std()), 1e-12)
+    return shift.astype(np.float32), scale.astype(np.float32), out_scale
+
+
+def train_closure(raw, targets, epochs=30, batch=8192, lr=2e-3, seed=5, device=0):
+    shift, scale, out_scale = normalise(raw, targets)
+    x = ((raw - shift) * scale).astype(np.float32)
+    t = (targets / out_scale).astype(np.float32)
+    tr = MlpTrainer(x, t, seed=seed, device=device)
+    loss0, _ = tr.loss_grad()
+    losses = tr.train(epochs, batch, lr)
+    params = tr.params()
+    tr.close()
+    return {"params": params, "shift": shift, "scale": scale, "out_scale": out_scale,
+            "loss_initial": loss0, "losses": losses}
+
+
+def run_coarse(cx, cy, cz, u_in, re, noise_amp, steps, closure=None, cs=0.0, precision="f32",
+               device=0, seed=11, tau_min=None):
+    g, p = channel(cx, cy, cz, u_in, re, cy, cs=cs)
+    part = TLBMPartition.from_arrays(problem_from_params(p), g.nd_type, precision=precision,
+                                     arithmetic="fast", device=device)
+    part.set_inlet_profile(u_in * (1.0 + noise_amp * inlet_noise(cx, cy, 1, seed=seed)))
+    nu = (1.0 / p.omega - 0.5) / 3.0
+    if closure is not None:
+        part.set_closure_mlp(closure["params"], closure["scale"], closure["shift"],
+                             closure["out_scale"], tau_min if tau_min else 3.0 * nu + 0.5 + 1e-6)
+    ms = part.time_steps(0, steps)
+    ux, uy, uz, rho = part.macros()
+    part.close()
+    return {"uz": uz.reshape(cz, cy, cx), "ms": ms, "finite": bool(np.isfinite(uz).all()),
+            "nd": g.nd_type.reshape(cz, cy, cx)}
+
+
+def evaluate(run, ref_uz, z_planes):
+    prof = rel_l2(mean_profile(run["uz"], run["nd"]), ref_uz.mean(axis=(1, 2)))
+    e_run = spectrum(run["uz"], z_planes)[1:]
+    e_ref = spectrum(ref_uz, z_planes)[1:]
+    spec = rel_l2(np.log(e_run + 1e-30), np.log(e_ref + 1e-30))
+    return {"profile_err": prof, "spectrum_log_err": spec, "finite": run["finite"],
+            "ms_per_step": run["ms"]}
+
+
+def study(cx=128, cy=64, cz=64, factor=4, u_in=0.05, re=3000.0, noise_amp=0.01,
+          coarse_steps=1024, snap_every=64, train_from=512, epochs=30, device=0, seed=11):
+    """The learned-closure experiment; returns errors of Smagorinsky and the learned closure
+    against the filtered fine run at `coarse_steps`, and their costs per step."""
+    snaps, omega_f = run_fine(cx, cy, cz, factor, u_in, re, noise_amp, coarse_steps, snap_every,
+                              device=device, seed=seed)
+    nu_c = u_in * cy / re
+    train = {k: v for k, v in snaps.items() if train_from <= k < coarse_steps}
+    raw, nut = build_dataset(train, nu_c, nu_cap=50.0 * nu_c)
+    cl = train_closure(raw, nut, epochs=epochs, device=device)
+    ref = snaps[coarse_steps]["uz"].astype(np.float64)
+    zp = list(range(cz // 2, cz - 2, max(1, cz // 16)))
+    out = {"samples": int(len(nut)), "nu_t_mean": float(nut.mean()),
+           "loss_initial": float(cl["loss_initial"]), "loss_final": float(cl["losses"][-1])}
+    for name, kw in (("smagorinsky", {"cs": 0.1}), ("learned", {"closure": cl}),
+                     ("none", {})):
+        r = run_coarse(cx, cy, cz, u_in, re, noise_amp, coarse_steps, device=device, seed=seed,
+                       **kw)
+        out[name] = evaluate(r, ref, zp)
+    return out, cl

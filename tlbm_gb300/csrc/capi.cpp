@@ -235,6 +235,18 @@ tlbm_status tlbm_mass(tlbm_handle* h, double* mass) {
 }
 int64_t tlbm_kernel_launches(const tlbm_handle* h) { return valid(h) ? h->engine->launches() : -1; }
 
+tlbm_status tlbm_set_inlet_profile(tlbm_handle* h, const double* uz) {
+  TLBM_CALL(h, h->engine->set_inlet_profile(uz));
+}
+tlbm_status tlbm_set_closure_mlp(tlbm_handle* h, const float* params, const float* scale,
+                                 const float* shift, float out_scale, float tau_min) {
+  TLBM_CALL(h, h->engine->set_closure(params, scale, shift, out_scale, tau_min));
+}
+tlbm_status tlbm_filtered_fields(tlbm_handle* h, int factor, void* out) {
+  if (!out) return TLBM_ERR_INVALID_ARGUMENT;
+  TLBM_CALL(h, h->engine->filtered(factor, out));
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------- ensembles

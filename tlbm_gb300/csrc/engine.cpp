@@ -22,6 +22,9 @@
 #include <fstream>
 #include <sstream>
 
+#include "mlp.cuh"
+#include "mlp_kernels.h"
+
 namespace tlbm {
 
 // ----------------------------------------------------------------------------- input parsing
@@ -220,8 +223,19 @@ Engine::~Engine() {
   cudaFree(d_order_);
   cudaFree(d_partial_);
   cudaFree(d_mass_);
+  cudaFree(d_inlet_d_);
+  cudaFree(d_inlet_f_);
+  cudaFree(d_closure_);
+  cudaFree(d_closure_w_);
   if (h_pinned_) cudaFreeHost(h_pinned_);
   if (stream_) cudaStreamDestroy(stream_);
+}
+
+void Engine::drop_graphs() {
+  for (auto& g : graph_) {
+    if (g) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
 }
 
 Status Engine::create(const tlbm_problem& prob, const int32_t* nd_type, const int32_t* parts,
@@ -445,6 +459,7 @@ Status Engine::enqueue_step(int is_even) {
     }
     TLBM_CUDA(launch_step_ref(q_, sb_, a, launch_));
   } else {
+    a.closure = d_closure_;
     TLBM_CUDA(launch_step_fast(q_, store_, a, launch_));
     if (has_type5_) ++launches_;
   }
@@ -660,6 +675,86 @@ Status Engine::mass(double* out) {
   TLBM_CUDA(cudaStreamSynchronize(stream_));
   if (!std::isfinite(*out))
     return Status::err(TLBM_ERR_NUMERIC, "total mass is not finite: the run has diverged");
+  return Status::ok();
+}
+
+Status Engine::set_inlet_profile(const double* uz) {
+  TLBM_CUDA(cudaSetDevice(opt_.device));
+  if (ref_arith_)
+    return Status::err(TLBM_ERR_UNSUPPORTED,
+                       "an inlet profile changes the reference's physics: fast arithmetic only");
+  TLBM_CUDA(cudaStreamSynchronize(stream_));
+  drop_graphs();
+  if (!uz) {
+    pb_.inlet_d = nullptr;
+    pb_.inlet_f = nullptr;
+    return Status::ok();
+  }
+  const size_t nxy = static_cast<size_t>(pb_.nxy);
+  std::vector<float> uf(nxy);
+  for (size_t k = 0; k < nxy; ++k) uf[k] = static_cast<float>(uz[k]);
+  if (!d_inlet_d_) TLBM_CUDA(cudaMalloc(&d_inlet_d_, nxy * sizeof(double)));
+  if (!d_inlet_f_) TLBM_CUDA(cudaMalloc(&d_inlet_f_, nxy * sizeof(float)));
+  TLBM_CUDA(cudaMemcpy(d_inlet_d_, uz, nxy * sizeof(double), cudaMemcpyHostToDevice));
+  TLBM_CUDA(cudaMemcpy(d_inlet_f_, uf.data(), nxy * sizeof(float), cudaMemcpyHostToDevice));
+  pb_.inlet_d = d_inlet_d_;
+  pb_.inlet_f = d_inlet_f_;
+  return Status::ok();
+}
+
+Status Engine::set_closure(const float* params, const float* scale, const float* shift,
+                           float out_scale, float tau_min) {
+  TLBM_CUDA(cudaSetDevice(opt_.device));
+  if (ref_arith_)
+    return Status::err(TLBM_ERR_UNSUPPORTED,
+                       "the learned closure has no reference arithmetic: use TLBM_ARITH_FAST");
+  TLBM_CUDA(cudaStreamSynchronize(stream_));
+  drop_graphs();
+  if (!params) {
+    cudaFree(d_closure_);
+    d_closure_ = nullptr;
+    return Status::ok();
+  }
+  if (!scale || !shift || !(tau_min > 0.5f) || !std::isfinite(out_scale))
+    return Status::err(TLBM_ERR_INVALID_ARGUMENT,
+                       "closure needs 8 scales and shifts, a finite out_scale and tau_min > 1/2");
+  // weights rounded to BF16 once here; biases stay FP32 (mlp.cuh)
+  std::vector<float> w(params, params + mlp::kParams);
+  for (int p = 0; p < mlp::kParams; ++p) {
+    const bool bias = (p >= mlp::oB1 && p < mlp::oW2) || (p >= mlp::oB2 && p < mlp::oW3) ||
+                      p == mlp::oB3;
+    if (!bias) w[p] = mlp::bf16r(w[p]);
+  }
+  if (!d_closure_w_) TLBM_CUDA(cudaMalloc(&d_closure_w_, mlp::kParams * sizeof(float)));
+  TLBM_CUDA(cudaMemcpy(d_closure_w_, w.data(), mlp::kParams * sizeof(float),
+                       cudaMemcpyHostToDevice));
+  mlp::Closure c{};
+  c.w = d_closure_w_;
+  for (int k = 0; k < mlp::kIn; ++k) {
+    c.scale[k] = scale[k];
+    c.shift[k] = shift[k];
+  }
+  c.out_scale = out_scale;
+  c.tau_min = tau_min;
+  if (!d_closure_) TLBM_CUDA(cudaMalloc(&d_closure_, sizeof(mlp::Closure)));
+  TLBM_CUDA(cudaMemcpy(d_closure_, &c, sizeof(c), cudaMemcpyHostToDevice));
+  return Status::ok();
+}
+
+Status Engine::filtered(int f, void* out) {
+  TLBM_CUDA(cudaSetDevice(opt_.device));
+  if (f < 1 || prob_.nx % f || prob_.ny % f || prob_.nz % f)
+    return Status::err(TLBM_ERR_INVALID_ARGUMENT, "the filter width must divide nx, ny and nz");
+  TLBM_TRY(compute_outputs());
+  const size_t nc = static_cast<size_t>(prob_.nx / f) * (prob_.ny / f) * (prob_.nz / f);
+  void* d = nullptr;
+  TLBM_CUDA(cudaMallocAsync(&d, 10 * nc * ob_, stream_));
+  cudaError_t e = launch_box_filter(d_macro_, ob_, prob_.nx, prob_.ny, prob_.nz, f, d, stream_);
+  ++launches_;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, 10 * nc * ob_, cudaMemcpyDeviceToHost, stream_);
+  cudaFreeAsync(d, stream_);
+  TLBM_CUDA(e);
+  TLBM_CUDA(cudaStreamSynchronize(stream_));
   return Status::ok();
 }
 

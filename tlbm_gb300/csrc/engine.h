@@ -51,6 +51,13 @@ class Engine {
   Status copy_populations(int which, void* out);
   Status copy_adjacency(int32_t* out);
   Status mass(double* out);
+  // per-(x, y) inlet velocity of the z = 0 plane (nx*ny values); null restores u_bc
+  Status set_inlet_profile(const double* uz);
+  // learned closure (mlp.cuh); params null removes it
+  Status set_closure(const float* params, const float* scale, const float* shift,
+                     float out_scale, float tau_min);
+  // box filter by f of the last step's macroscopic fields: 10 coarse fields (mlp_kernels.h)
+  Status filtered(int f, void* out);
 
   const tlbm_problem& problem() const { return prob_; }
   int output_bytes() const { return ob_; }
@@ -98,6 +105,11 @@ class Engine {
   double* d_mass_ = nullptr;
   void* h_pinned_ = nullptr;
   cudaGraphExec_t graph_[2] = {nullptr, nullptr};
+  void drop_graphs();
+  double* d_inlet_d_ = nullptr;
+  float* d_inlet_f_ = nullptr;
+  void* d_closure_ = nullptr;    // mlp::Closure
+  float* d_closure_w_ = nullptr;  // its weights
 
   int last_src_ = -1, last_dst_ = -1;
   bool outputs_fresh_ = false;

@@ -28,6 +28,9 @@ struct DevProblem {
   // byte offset, from a cell's own population of speed 0, of the population of speed i that an
   // interior cell (no face of the box) pulls: i*n*bytes - (ex + ey*nx + ez*nx*ny)*bytes
   long long pull_off[27];
+  // optional inlet velocity per (x, y) of the z = 0 plane (nx*ny values; null: uniform u_bc)
+  const double* inlet_d;
+  const float* inlet_f;
 };
 
 // problem parameters in the compute type
@@ -40,6 +43,9 @@ struct Par<double> {
   static TLBM_HD double u_bc(const DevProblem& p) { return p.u_bc; }
   static TLBM_HD double rho_bc(const DevProblem& p) { return p.rho_bc; }
   static TLBM_HD double nu(const DevProblem& p) { return p.nu; }
+  static TLBM_HD double u_in(const DevProblem& p, int xy) {
+    return p.inlet_d ? p.inlet_d[xy] : p.u_bc;
+  }
 };
 template <>
 struct Par<float> {
@@ -48,6 +54,9 @@ struct Par<float> {
   static TLBM_HD float u_bc(const DevProblem& p) { return p.u_bc_f; }
   static TLBM_HD float rho_bc(const DevProblem& p) { return p.rho_bc_f; }
   static TLBM_HD float nu(const DevProblem& p) { return p.nu_f; }
+  static TLBM_HD float u_in(const DevProblem& p, int xy) {
+    return p.inlet_f ? p.inlet_f[xy] : p.u_bc_f;
+  }
 };
 
 // fills the float copies and the interior pull offsets of `pb` for q speeds of `bytes` each

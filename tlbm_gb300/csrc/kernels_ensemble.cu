@@ -30,14 +30,14 @@ __global__ void __launch_bounds__(256) k_ensemble_step(EnsembleArgs a) {
       if (x >= s.pb.nx) break;
       if (ch.q == 19) {
         if (s.pb.cs > 0)
-          cell_step<Lattice<19>, K, true>(s, x, y, z);
+          cell_step<Lattice<19>, K, fast::kClosureSmag>(s, x, y, z);
         else
-          cell_step<Lattice<19>, K, false>(s, x, y, z);
+          cell_step<Lattice<19>, K, fast::kClosureNone>(s, x, y, z);
       } else {
         if (s.pb.cs > 0)
-          cell_step<Lattice<15>, K, true>(s, x, y, z);
+          cell_step<Lattice<15>, K, fast::kClosureSmag>(s, x, y, z);
         else
-          cell_step<Lattice<15>, K, false>(s, x, y, z);
+          cell_step<Lattice<15>, K, fast::kClosureNone>(s, x, y, z);
       }
     }
   }

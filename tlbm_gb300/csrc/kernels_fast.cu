@@ -10,13 +10,28 @@
 namespace tlbm {
 namespace {
 
-template <class L, int K, bool kSmag>
+template <class L, int K, int kClosure>
 __global__ void __launch_bounds__(128) k_step_fast(StepArgs a) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
   if (x >= a.pb.nx || y >= a.pb.ny) return;
-  cell_step<L, K, kSmag>(a, x, y, z);
+  cell_step<L, K, kClosure>(a, x, y, z);
+}
+
+// learned closure: the network's weights are staged in shared memory once per block
+template <class L, int K>
+__global__ void __launch_bounds__(128) k_step_fast_mlp(StepArgs a) {
+  __shared__ float sw[mlp::kParams];
+  const mlp::Closure* cl = static_cast<const mlp::Closure*>(a.closure);
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+  for (int k = tid; k < mlp::kParams; k += blockDim.x * blockDim.y) sw[k] = cl->w[k];
+  __syncthreads();
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= a.pb.nx || y >= a.pb.ny) return;
+  cell_step<L, K, fast::kClosureMlp>(a, x, y, z, sw);
 }
 
 template <class L, int K>
@@ -38,7 +53,7 @@ __global__ void __launch_bounds__(128) k_macros_fast(DevProblem pb,
   C f[L::Q];
   unpack<L, K>(raw, f);
   C rho, ux, uy, uz;
-  node_macros<L, C>(pb.nd_type[c], f, static_cast<C>(pb.u_bc), static_cast<C>(pb.rho_bc), rho, ux,
+  node_macros<L, C>(pb.nd_type[c], f, Par<C>::u_in(pb, c % pb.nxy), Par<C>::rho_bc(pb), rho, ux,
                     uy, uz);
   ux_o[c] = ux;
   uy_o[c] = uy;
@@ -60,7 +75,7 @@ __global__ void k_quirk_fast(DevProblem pb, const typename Store<K>::T* __restri
   C f[L::Q];
   unpack<L, K>(raw, f);
   C rho, ux, uy, uz;
-  node_macros<L, C>(pb.nd_type[c], f, static_cast<C>(pb.u_bc), static_cast<C>(pb.rho_bc), rho, ux,
+  node_macros<L, C>(pb.nd_type[c], f, Par<C>::u_in(pb, c % pb.nxy), Par<C>::rho_bc(pb), rho, ux,
                     uy, uz);
   uy_out[c] = uy;
 }
@@ -110,10 +125,12 @@ dim3 grid_of(const DevProblem& pb, const Launch& l) {
 template <class L, int K>
 cudaError_t step_lk(const StepArgs& a, const Launch& l) {
   const dim3 g = grid_of(a.pb, l), b(l.bx, l.by, 1);
-  if (a.pb.cs > 0)
-    k_step_fast<L, K, true><<<g, b, 0, l.stream>>>(a);
+  if (a.closure)
+    k_step_fast_mlp<L, K><<<g, b, 0, l.stream>>>(a);
+  else if (a.pb.cs > 0)
+    k_step_fast<L, K, fast::kClosureSmag><<<g, b, 0, l.stream>>>(a);
   else
-    k_step_fast<L, K, false><<<g, b, 0, l.stream>>>(a);
+    k_step_fast<L, K, fast::kClosureNone><<<g, b, 0, l.stream>>>(a);
   return cudaGetLastError();
 }
 

@@ -53,8 +53,11 @@ __device__ __forceinline__ void node_macros(uint8_t t, const C (&f)[L::Q], C u_b
   }
 }
 
-template <class L, int K, bool kSmag>
-__device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z) {
+// kClosure: fast::kClosureNone (BGK), kClosureSmag, kClosureMlp (sw = the closure's weights
+// in shared memory; boundary nodes then use Smagorinsky when cs > 0)
+template <class L, int K, int kClosure>
+__device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z,
+                                          const float* sw = nullptr) {
   using S = Store<K>;
   using C = typename S::C;
   using T = typename S::T;
@@ -80,8 +83,9 @@ __device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z
   if (t == kFluid) {
     C f[L::Q];
     unpack<L, K>(raw, f);
-    fast::fluid_collide<L, C, kSmag>(f, Par<C>::omega(pb), Par<C>::cs(pb), Par<C>::nu(pb),
-                                     pb.dynamics == 1, rho, ux, uy, uz);
+    fast::fluid_collide<L, C, kClosure>(f, Par<C>::omega(pb), Par<C>::cs(pb), Par<C>::nu(pb),
+                                        pb.dynamics == 1, rho, ux, uy, uz,
+                                        static_cast<const mlp::Closure*>(a.closure), sw);
 #pragma unroll
     for (int i = 0; i < L::Q; ++i) dst[i * n + c] = S::save(f[i], fast::wgt<L, C>(i));
   } else if (t == kSolid) {
@@ -95,7 +99,7 @@ __device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z
   } else {
     C f[L::Q];
     unpack<L, K>(raw, f);
-    const C u_bc = Par<C>::u_bc(pb);
+    const C u_bc = (t == kInlet) ? Par<C>::u_in(pb, x + y * pb.nx) : Par<C>::u_bc(pb);
     node_macros<L, C>(t, f, u_bc, Par<C>::rho_bc(pb), rho, ux, uy, uz);
     if constexpr (S::kShifted) {
       // 16-bit storage: the inlet density and outlet velocity sums are taken in FP64
@@ -106,7 +110,8 @@ __device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z
           fd[i] = static_cast<double>(fast::wgt<L, float>(i)) +
                   static_cast<double>(S::load(raw[i], 0.0f));
         if (t == kInlet)
-          rho = static_cast<C>(fast::inlet_rho<L, double>(fd, 1.0 / (1.0 - pb.u_bc)));
+          rho = static_cast<C>(fast::inlet_rho<L, double>(
+              fd, 1.0 / (1.0 - Par<double>::u_in(pb, x + y * pb.nx))));
         else
           uz = static_cast<C>(fast::outlet_uz<L, double>(fd, 1.0 / pb.rho_bc));
       }
@@ -127,7 +132,7 @@ __device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z
     if (t == kOutlet) fast::nebb<L, C, false>(f, feq);
     if (pb.dynamics == 1) {
       C om = Par<C>::omega(pb);
-      if constexpr (kSmag)
+      if (kClosure == fast::kClosureSmag || (kClosure == fast::kClosureMlp && pb.cs > 0))
         om = fast::smagorinsky_omega<L, C>(f, feq, Par<C>::cs(pb), Par<C>::nu(pb));
       fast::relax<L, C>(f, feq, om);
     }
