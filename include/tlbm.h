@@ -182,6 +182,15 @@ tlbm_status tlbm_mass(tlbm_handle* h, double* mass);
 /* Number of kernels this handle has launched since creation. */
 int64_t tlbm_kernel_launches(const tlbm_handle* h);
 
+/* Replaces load_restart_data (src/TLBM_Partition.cpp:481-540): sets both population buffers
+ * to the equilibrium of the given macroscopic fields (float, global order, nx*ny*nz values
+ * each), computed in the handle's arithmetic.  tlbm_create does this itself when params.lbm
+ * line 14 is 1, reading the fields from restart_ux.b_dat, restart_uy.b_dat, restart_uz.b_dat
+ * and restart_rho.b_dat (raw float32) -- the datasets of the reference's restart.h5, which is
+ * HDF5 and is not read here. */
+tlbm_status tlbm_load_restart(tlbm_handle* h, const float* ux, const float* uy, const float* uz,
+                              const float* rho);
+
 /* ---- inflow, learned closure, filtering --------------------------------------------------
  * No counterpart in the reference (its inlet velocity is the scalar uLBM,
  * src/TLBM_Partition.cpp:765-766, and its only closure is Smagorinsky).  Fast arithmetic only. */

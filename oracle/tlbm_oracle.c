@@ -450,6 +450,23 @@ void oracle_step(oracle_state* s, int is_even) {
   }
 }
 
+/* load_restart_data (src/TLBM_Partition.cpp:481-540): the restart fields are read as float
+ * (NATIVE_FLOAT) into `real` macroscopic arrays, then both population buffers are set to
+ * compute_equilibrium of them, node by node. */
+void oracle_load_restart(oracle_state* s, const float* ux, const float* uy, const float* uz,
+                         const float* rho) {
+  for (int64_t nd = 0; nd < s->n; ++nd) {
+    s->ux[nd] = ux[nd];
+    s->uy[nd] = uy[nd];
+    s->uz[nd] = uz[nd];
+    s->rho[nd] = rho[nd];
+  }
+  for (int64_t nd = 0; nd < s->n; ++nd) {
+    equilibrium(s, s->f_even, nd);
+    equilibrium(s, s->f_odd, nd);
+  }
+}
+
 /* run steps first_ts .. first_ts+nsteps-1 with take_LBM_time_step(ts % 2) */
 void oracle_run(oracle_state* s, int first_ts, int nsteps) {
   for (int ts = first_ts; ts < first_ts + nsteps; ++ts) oracle_step(s, ts % 2);
@@ -603,6 +620,30 @@ int oracle_run_dir(const char* dir, int nthreads, double* elapsed) {
   oracle_state* s = oracle_create(q, p.dynamics, p.cs, p.rho_lbm, p.u_lbm, p.omega, p.nx, p.ny,
                                   p.nz, nd, p.time_avg);
   oracle_set_threads(s, nthreads);
+  if (p.restart) {
+    /* restart fields as raw float32 files in global order (the reference's restart.h5 holds
+     * the same datasets: velocity/x,y,z and density/rho) */
+    static const char* names[4] = {"restart_ux.b_dat", "restart_uy.b_dat", "restart_uz.b_dat",
+                                   "restart_rho.b_dat"};
+    float* r[4] = {NULL, NULL, NULL, NULL};
+    int ok = 1;
+    for (int k = 0; k < 4; ++k) {
+      char path[4096];
+      snprintf(path, sizeof(path), "%s/%s", dir, names[k]);
+      FILE* fh = fopen(path, "rb");
+      r[k] = (float*)malloc(sizeof(float) * (size_t)n);
+      if (!fh || fread(r[k], sizeof(float), (size_t)n, fh) != (size_t)n) ok = 0;
+      if (fh) fclose(fh);
+    }
+    if (ok) oracle_load_restart(s, r[0], r[1], r[2], r[3]);
+    for (int k = 0; k < 4; ++k) free(r[k]);
+    if (!ok) {
+      oracle_destroy(s);
+      free(nd);
+      free(parts);
+      return -5;
+    }
+  }
   int64_t* order = output_order(parts, n, nparts);
   int32_t* ord32 = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
   for (int64_t k = 0; k < n; ++k) ord32[k] = (int32_t)order[k];

@@ -50,6 +50,7 @@ def lib(prec: str = "f64"):
     L.oracle_run_dir.argtypes = [ctypes.c_char_p, i32, ctypes.POINTER(dbl)]
     L.oracle_run_dir.restype = i32
     L.oracle_real_bytes.restype = i32
+    L.oracle_load_restart.argtypes = [vp, vp, vp, vp, vp]
     _LIBS[prec] = L
     return L
 
@@ -78,6 +79,10 @@ class Oracle:
             raise ValueError("oracle_create failed")
         self.L.oracle_set_threads(self.h, threads)
         self.ts = 0
+
+    def load_restart(self, ux, uy, uz, rho) -> None:
+        arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in (ux, uy, uz, rho)]
+        self.L.oracle_load_restart(self.h, *[a.ctypes.data for a in arrs])
 
     def run(self, nsteps: int) -> None:
         self.L.oracle_run(self.h, self.ts, nsteps)

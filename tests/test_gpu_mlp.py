@@ -130,8 +130,9 @@ def test_closure_pipeline_small():
     """A miniature run of the whole pipeline (fine 64x32x32 -> coarse 32x16x16): the network
     trains on the GPU, the learned closure runs fused in collide, and its errors against the
     filtered fine run are reported next to Smagorinsky's and plain BGK's."""
-    out, cl = CL.study(cx=32, cy=16, cz=16, factor=2, u_in=0.05, re=600.0, coarse_steps=256,
+    out, cl = CL.study(cx=32, cy=16, cz=16, factor=2, u_in=0.05, re=200.0, coarse_steps=256,
                        snap_every=32, train_from=96, epochs=15)
     print(out)
+    assert out["fine_finite"]
     assert out["loss_final"] < out["loss_initial"]
     assert out["learned"]["finite"] and out["smagorinsky"]["finite"]

@@ -234,3 +234,47 @@ def test_diverged_run_reports_numeric_error():
     with pytest.raises(T.TLBMError) as e:
         part.mass()
     assert e.value.status == T.ERR_NUMERIC
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+@pytest.mark.parametrize("q", [19, 27])
+def test_restart_matches_oracle(q, prec):
+    """tlbm_load_restart (load_restart_data) from arbitrary fields, then 7 steps: bit-identical
+    populations and fields to the oracle (reference arithmetic)."""
+    geom, p = small_problem(q, nx=9, ny=7, nz=8, seed=q + 1)
+    rng = np.random.default_rng(4)
+    n = geom.num_nodes
+    f = [rng.uniform(-0.03, 0.03, n), rng.uniform(-0.03, 0.03, n), rng.uniform(0.0, 0.06, n),
+         rng.uniform(0.97, 1.03, n)]
+    part = T.TLBMPartition.from_arrays(T.problem_from_params(p), geom.nd_type, precision=prec,
+                                       arithmetic="reference")
+    part.load_restart(*f)
+    o = oracle_lib.Oracle(q, 1, p.cs, p.rho_lbm, p.u_lbm, p.omega, geom.nx, geom.ny, geom.nz,
+                          geom.nd_type, prec=prec)
+    o.load_restart(*f)
+    for ts in range(7):
+        part.take_LBM_time_step(ts % 2)
+    o.run(7)
+    assert np.array_equal(part.populations(0), o.populations(0))
+    for a, b in zip(part.macros(), o.macros()):
+        assert np.array_equal(a, b)
+
+
+def test_restart_from_dump_files(tmp_path):
+    """A run dumps, tLBM_create_restart's datasets are written from the dump, and a restarted run
+    through tLBMexec writes the same files as the oracle restarted from them."""
+    from tlbm_gb300 import io as TIO
+
+    geom, p = small_problem(19, nx=12, ny=10, nz=14, seed=9)
+    p.num_ts, p.plot_freq = 20, 20
+    d0, d1, d2 = (str(tmp_path / s) for s in ("first", "gpu", "cpu"))
+    G.write_inputs(d0, geom, p)
+    T.run_like_tlbmexec(T.TLBMPartition(d0, precision="f32", arithmetic="reference"))
+    p.restart = 1
+    for d in (d1, d2):
+        G.write_inputs(d, geom, p)
+        TIO.create_restart(d0, 0, d)
+    r = subprocess.run([B.EXE], cwd=d1, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    oracle_lib.run_dir(d2, "f32")
+    assert output_digests(d1) == output_digests(d2)

@@ -107,6 +107,7 @@ def library(path: str = LIB_PATH):
         "tlbm_copy_adjacency": (i32, [H, vp]),
         "tlbm_mass": (i32, [H, ctypes.POINTER(ctypes.c_double)]),
         "tlbm_kernel_launches": (i64, [H]),
+        "tlbm_load_restart": (i32, [H, vp, vp, vp, vp]),
         "tlbm_set_inlet_profile": (i32, [H, vp]),
         "tlbm_set_closure_mlp": (i32, [H, vp, vp, vp, ctypes.c_float, ctypes.c_float]),
         "tlbm_filtered_fields": (i32, [H, i32, vp]),
@@ -276,6 +277,11 @@ class TLBMPartition:
 
     def kernel_launches(self) -> int:
         return self._L.tlbm_kernel_launches(self._h)
+
+    def load_restart(self, ux, uy, uz, rho) -> None:
+        """Populations = equilibrium of the given fields (load_restart_data)."""
+        arrs = [np.ascontiguousarray(a, dtype=np.float32).reshape(-1) for a in (ux, uy, uz, rho)]
+        _check(self._L.tlbm_load_restart(self._h, *[a.ctypes.data for a in arrs]), self._h)
 
     def set_inlet_profile(self, uz) -> None:
         """Inlet u_z per (x, y) of the z = 0 plane (None restores the uniform uLBM)."""

@@ -235,6 +235,11 @@ tlbm_status tlbm_mass(tlbm_handle* h, double* mass) {
 }
 int64_t tlbm_kernel_launches(const tlbm_handle* h) { return valid(h) ? h->engine->launches() : -1; }
 
+tlbm_status tlbm_load_restart(tlbm_handle* h, const float* ux, const float* uy, const float* uz,
+                              const float* rho) {
+  TLBM_CALL(h, h->engine->load_restart(ux, uy, uz, rho));
+}
+
 tlbm_status tlbm_set_inlet_profile(tlbm_handle* h, const double* uz) {
   TLBM_CALL(h, h->engine->set_inlet_profile(uz));
 }

@@ -413,15 +413,35 @@ Status Engine::init(const int32_t* nd_type, const int32_t* parts, int size) {
   TLBM_CUDA(cudaMalloc(&d_partial_, nb * sizeof(double)));
   TLBM_CUDA(cudaMalloc(&d_mass_, sizeof(double)));
 
-  if (prob_.restart_flag)
-    return Status::err(TLBM_ERR_UNSUPPORTED,
-                       "restart (params.lbm line 14) needs restart data; not available here");
   // f = w*rho in both buffers (initialize_data_arrays, src/TLBM_Partition.cpp:458-465)
   for (auto p : d_f_) {
     TLBM_CUDA(launch_init_uniform(q_, store_, pb_, p, prob_.rho_lbm, launch_));
     ++launches_;
   }
   TLBM_CUDA(cudaStreamSynchronize(stream_));
+  if (prob_.restart_flag) {
+    // load_restart_data (src/TLBM_Partition.cpp:481-540) reads restart.h5; the same four
+    // datasets are read here as raw float32 files in global node order
+    if (workdir_.empty())
+      return Status::err(TLBM_ERR_INVALID_ARGUMENT,
+                         "restart flag set without a directory: use tlbm_load_restart");
+    const char* names[4] = {"restart_ux.b_dat", "restart_uy.b_dat", "restart_uz.b_dat",
+                            "restart_rho.b_dat"};
+    std::vector<std::vector<float>> r(4);
+    for (int k = 0; k < 4; ++k) {
+      std::string bytes;
+      Status s = read_text(workdir_ + "/" + names[k], &bytes);
+      if (!s.good())
+        return Status::err(TLBM_ERR_IO, std::string("restart data: ") + s.msg +
+                                            " (restart.h5 is HDF5, not read here; write the four "
+                                            "datasets as restart_{ux,uy,uz,rho}.b_dat)");
+      if (bytes.size() != n * sizeof(float))
+        return Status::err(TLBM_ERR_FORMAT, std::string(names[k]) + " must hold nx*ny*nz floats");
+      r[k].resize(n);
+      std::memcpy(r[k].data(), bytes.data(), bytes.size());
+    }
+    TLBM_TRY(load_restart(r[0].data(), r[1].data(), r[2].data(), r[3].data()));
+  }
   TLBM_CUDA(cudaMallocHost(&h_pinned_, n * std::max(ob_, 4)));
 
   // write_node_ordering (src/TLBM_Partition.cpp:542-561)
@@ -675,6 +695,33 @@ Status Engine::mass(double* out) {
   TLBM_CUDA(cudaStreamSynchronize(stream_));
   if (!std::isfinite(*out))
     return Status::err(TLBM_ERR_NUMERIC, "total mass is not finite: the run has diverged");
+  return Status::ok();
+}
+
+Status Engine::load_restart(const float* ux, const float* uy, const float* uz,
+                            const float* rho) {
+  TLBM_CUDA(cudaSetDevice(opt_.device));
+  if (!ux || !uy || !uz || !rho) return Status::err(TLBM_ERR_INVALID_ARGUMENT, "NULL field");
+  TLBM_CUDA(cudaStreamSynchronize(stream_));
+  const size_t bytes = static_cast<size_t>(n_) * sizeof(float);
+  void* d = nullptr;
+  TLBM_CUDA(cudaMalloc(&d, 4 * bytes));
+  char* db = static_cast<char*>(d);
+  const void* m[4] = {db, db + bytes, db + 2 * bytes, db + 3 * bytes};
+  const float* h[4] = {ux, uy, uz, rho};
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < 4 && e == cudaSuccess; ++k)
+    e = cudaMemcpy(const_cast<void*>(m[k]), h[k], bytes, cudaMemcpyHostToDevice);
+  // f = feq of every node, placed so that the next pull returns it at its own node
+  for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+    e = launch_init_equilibrium(q_, store_, pb_, d_f_[b], m, 4, launch_);
+    ++launches_;
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream_);
+  cudaFree(d);
+  TLBM_CUDA(e);
+  last_src_ = last_dst_ = -1;
+  outputs_fresh_ = false;
   return Status::ok();
 }
 

@@ -51,6 +51,8 @@ class Engine {
   Status copy_populations(int which, void* out);
   Status copy_adjacency(int32_t* out);
   Status mass(double* out);
+  // both population buffers = feq(u, rho) of the given float fields (load_restart_data)
+  Status load_restart(const float* ux, const float* uy, const float* uz, const float* rho);
   // per-(x, y) inlet velocity of the z = 0 plane (nx*ny values); null restores u_bc
   Status set_inlet_profile(const double* uz);
   // learned closure (mlp.cuh); params null removes it

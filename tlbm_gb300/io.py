@@ -1,0 +1,37 @@
+"""Output-file helpers: read dumps in global order and write restart data.
+
+The solver writes each field in partition-major order with ``ordering.b_dat`` giving the global
+node number of every position (src/TLBM_Partition.cpp:542-561, :608-683).  The reference's
+``tLBM_create_restart.py`` (python/tLBM_create_restart.py:34-68) un-permutes dump n and stores
+velocity/{x,y,z} and density/rho in ``restart.h5``; ``create_restart`` stores the same four
+datasets as raw float32 files (``restart_{ux,uy,uz,rho}.b_dat``), which the engine reads when
+params.lbm line 14 is 1 (HDF5 is not available to it).
+"""
+
+from __future__ import annotations
+
+import os
+
+import numpy as np
+
+
+def read_dump(workdir: str, dump: int, dtype=np.float32, fields=("ux", "uy", "uz", "density")):
+    """Fields of dump `dump` in global node order (the un-permutation of processTLBM.py)."""
+    order = np.fromfile(os.path.join(workdir, "ordering.b_dat"), dtype=np.int32)
+    out = {}
+    for f in fields:
+        a = np.fromfile(os.path.join(workdir, "%s%d.b_dat" % (f, dump)), dtype=dtype)
+        g = np.zeros_like(a)
+        g[order] = a
+        out[f] = g
+    return out
+
+
+def create_restart(workdir: str, dump: int, out_dir: str | None = None, dtype=np.float32):
+    """Write restart_{ux,uy,uz,rho}.b_dat (float32, global order) from dump `dump`."""
+    out_dir = out_dir or workdir
+    d = read_dump(workdir, dump, dtype)
+    os.makedirs(out_dir, exist_ok=True)
+    for src, dst in (("ux", "ux"), ("uy", "uy"), ("uz", "uz"), ("density", "rho")):
+        d[src].astype(np.float32).tofile(os.path.join(out_dir, "restart_%s.b_dat" % dst))
+    return out_dir
