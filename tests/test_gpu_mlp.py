@@ -136,3 +136,55 @@ def test_closure_pipeline_small():
     assert out["fine_finite"]
     assert out["loss_final"] < out["loss_initial"]
     assert out["learned"]["finite"] and out["smagorinsky"]["finite"]
+
+
+def test_fused_tensor_core_closure_matches_oracle():
+    """One step of the fused collide kernel with a random network, from a non-equilibrium state
+    on an all-fluid periodic box, against the closure computed in numpy: moments, Pi_neq,
+    normalised features, the BF16-rounded network (mlp_oracle), tau = 3 (nu + s y) + 1/2 and the
+    BGK relaxation.  The network runs on the tensor cores in the kernel (mma.sync, FP32
+    accumulation in another order), so the tolerance covers summation-order differences only:
+    a wrong network output moves the populations by ~1e-5."""
+    nx, ny, nz = 64, 8, 6
+    g = G.Geometry(nx, ny, nz, np.zeros(nx * ny * nz, np.int32))
+    p = G.params_lattice_units(g, "D3Q19", 0.05, 60.0, 6.0, 10)
+    p.omega = 1.6
+    n = g.num_nodes
+    part = T.TLBMPartition.from_arrays(T.problem_from_params(p), g.nd_type, precision="f32",
+                                       arithmetic="fast")
+    rng = np.random.default_rng(12)
+    part.load_restart(rng.uniform(-0.04, 0.04, n), rng.uniform(-0.04, 0.04, n),
+                      rng.uniform(-0.04, 0.04, n), rng.uniform(0.99, 1.01, n))
+    part.run(0, 1)
+    f = part.populations(0).reshape(n, 19).astype(np.float64)  # input of the next step
+    # lattice vectors from the neighbour table (push target of an interior node)
+    c = 1 + nx + nx * ny
+    tgt = part.adjacency().reshape(n, 19)[c]
+    e = np.stack([tgt % nx - 1, (tgt // nx) % ny - 1, tgt // (nx * ny) - 1], axis=1)
+    w = np.array([{0: 1 / 3, 1: 1 / 18, 2: 1 / 36}[int(k)] for k in (e * e).sum(1)], np.float32)
+    w = w.astype(np.float64)
+    rho = f.sum(1)
+    u = (f @ e) / rho[:, None]
+    eu = u @ e.T
+    feq = w[None, :] * rho[:, None] * (1 + 3 * eu + 4.5 * eu ** 2 - 1.5 * (u * u).sum(1)[:, None])
+    d = f - feq
+    pairs = [(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]
+    pi = np.stack([(d * (e[:, a] * e[:, b])[None, :]).sum(1) for a, b in pairs], axis=1)
+    q = np.sqrt((pi[:, :3] ** 2).sum(1) + 2 * (pi[:, 3:] ** 2).sum(1))
+    raw = np.concatenate([pi, (rho - 1)[:, None], q[:, None]], axis=1)
+    shift = raw.mean(0).astype(np.float32)
+    scale = (1.0 / raw.std(0)).astype(np.float32)
+    x = ((raw.astype(np.float32) - shift) * scale).astype(np.float32)
+    params = M.init_params(21)
+    _, _, y = M.forward_backward(params, x, np.zeros(n))
+    out_scale = 0.01
+    nu = (1.0 / p.omega - 0.5) / 3.0
+    tau = np.maximum(3.0 * (nu + out_scale * y) + 0.5, 3.0 * nu + 0.5 + 1e-6)
+    assert np.ptp(tau) > 1e-3  # the network changes the rate from cell to cell
+    want = f - (1.0 / tau)[:, None] * d
+    part.set_closure_mlp(params, scale, shift, out_scale, 3.0 * nu + 0.5 + 1e-6)
+    part.run(1, 1)
+    got = part.populations(1).reshape(n, 19).astype(np.float64)
+    err = np.abs(got - want).max()
+    print("fused closure step: max |f - oracle| = %.2e" % err)
+    assert err <= 1e-6

@@ -111,6 +111,9 @@ def library(path: str = LIB_PATH):
         "tlbm_set_inlet_profile": (i32, [H, vp]),
         "tlbm_set_closure_mlp": (i32, [H, vp, vp, vp, ctypes.c_float, ctypes.c_float]),
         "tlbm_filtered_fields": (i32, [H, i32, vp]),
+        "tlbm_processed_fields": (i32, [H, i32, vp]),
+        "tlbm_write_processed_data": (i32, [H, i32]),
+        "tlbm_process_output_dir": (i32, [ctypes.c_char_p, i32, ctypes.POINTER(i32)]),
         "tlbm_mlp_num_params": (i32, []),
         "tlbm_mlp_create": (i32, [i64, vp, vp, ctypes.c_uint64, i32, PH]),
         "tlbm_mlp_destroy": (i32, [H]),
@@ -127,6 +130,16 @@ def library(path: str = LIB_PATH):
         fn.argtypes = args
     _lib = L
     return L
+
+
+def process_output_dir(workdir: str, device: int = 0) -> int:
+    """processTLBM.py for a finished run directory, on the GPU; returns the dumps processed."""
+    L = library()
+    done = ctypes.c_int(0)
+    st = L.tlbm_process_output_dir(workdir.encode(), device, ctypes.byref(done))
+    if st != 0:
+        raise TLBMError(st, L.tlbm_get_last_error(None).decode())
+    return done.value
 
 
 def declared_symbols(header: str = HEADER) -> list[str]:
@@ -313,6 +326,24 @@ class TLBMPartition:
         cz, cy, cx = p[2] // factor, p[1] // factor, p[0] // factor
         return {k: out[i * nc:(i + 1) * nc].reshape(cz, cy, cx)
                 for i, k in enumerate(self.FILTERED)}
+
+    PROCESSED = ("ux", "uy", "uz", "velmag", "Fx", "Fy", "Fz", "pressure")
+    PROCESSED_AVG = ("ux", "uy", "uz", "velmag", "pressure")
+
+    def processed_fields(self, time_avg: bool = False) -> dict:
+        """processTLBM.py's fields (physical units, pressure - pRef, |u|, forces) of the last
+        step, or of the time averages, computed on the GPU; (z, y, x) float32 arrays."""
+        nx, ny, nz = self._shape()
+        n = nx * ny * nz
+        names = self.PROCESSED_AVG if time_avg else self.PROCESSED
+        out = np.empty(len(names) * n, np.float32)
+        _check(self._L.tlbm_processed_fields(self._h, int(bool(time_avg)), out.ctypes.data),
+               self._h)
+        return {k: out[i * n:(i + 1) * n].reshape(nz, ny, nx) for i, k in enumerate(names)}
+
+    def write_processed_data(self, time_avg: bool = False) -> None:
+        """out{k}.bin + data{k}.xmf (or timeAvg.bin/.xmf) in the run directory."""
+        _check(self._L.tlbm_write_processed_data(self._h, int(bool(time_avg))), self._h)
 
     def _shape(self):
         if not hasattr(self, "_dims"):

@@ -38,6 +38,8 @@ UNITS = [
     ("kernels_ensemble.cu", []),
     ("ensemble.cpp", ["-x", "cu"]),
     ("kernels_mlp.cu", []),
+    ("kernels_post.cu", ["-fmad=false"]),
+    ("post.cpp", ["-x", "cu"]),
     ("mlp_trainer.cpp", ["-x", "cu"]),
     ("capi_mlp.cpp", ["-x", "cu"]),
     ("engine.cpp", ["-x", "cu"]),

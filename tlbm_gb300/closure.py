@@ -3,9 +3,14 @@ training, and evaluation against Smagorinsky on the box-filtered fine solution.
 
 Pipeline (all on the GPU except numpy bookkeeping on coarse-sized arrays):
 
-1. A fine run (factor `f` finer in space and time, plain BGK) with a seeded, smooth inlet
+1. A fine run (factor `f` finer in space and time) of a periodic-x/y box whose Zou-He inlet
+   carries a plane jet (u_in (1 + 0.5 J(y)), tanh shear layers) times a seeded, smooth 1 %
    perturbation; snapshots of its macroscopic fields are box-filtered on the device
-   (``tlbm_filtered_fields``) to the coarse grid: rho, u and the means of u_a u_b.
+   (``tlbm_filtered_fields``) to the coarse grid: rho, u and the means of u_a u_b.  The fine
+   run relaxes with a constant Smagorinsky coefficient fine_cs (default 0.05): plain BGK at
+   the fine tau = 0.5128 of Re = 3000 diverges within ~700 fine steps, first at the
+   non-equilibrium bounce-back outlet, once the inlet perturbation's pressure waves reach it
+   (measured with and without the perturbation: without it the run stays steady).
 2. Per coarse cell the least-squares eddy viscosity that makes the Boussinesq model reproduce
    the filtered sub-grid stress:  nu_t* = -(tau_sgs^dev : S) / (2 S : S),
    tau_sgs_ab = mean(u_a u_b) - mean(u_a) mean(u_b), S the strain rate of the filtered velocity
@@ -14,7 +19,8 @@ Pipeline (all on the GPU except numpy bookkeeping on coarse-sized arrays):
    its non-equilibrium stress Pi_ab = -2 rho c_s^2 tau* S_ab (first-order Chapman-Enskog),
    rho - 1 and |Pi| -- the same quantities the fused collide kernel computes from f - feq.
 4. The 8-32-32-1 network is trained on the GPU (``tlbm_mlp_*``: BF16 weights, FP32
-   accumulation, Adam) and installed with ``tlbm_set_closure_mlp``.
+   accumulation, Adam) and installed with ``tlbm_set_closure_mlp``; the collide kernel then
+   evaluates it on the tensor cores (mlp.cuh: forward_warp).
 5. Coarse runs with Smagorinsky (cs = 0.1) and with the learned closure are compared with the
    filtered fine run on the mean streamwise-velocity profile and on the 2-D energy spectrum of
    u_z in x-y planes.
@@ -51,6 +57,23 @@ def inlet_noise(nx: int, ny: int, factor: int = 1, modes: int = 24, seed: int = 
         out += rng.normal() * np.sin(2 * np.pi * (m * X + n * Y) + rng.uniform(0, 2 * np.pi))
     out -= out.mean()
     return out / out.std()
+
+
+def jet_profile(nx: int, ny: int, factor: int = 1, ratio: float = 0.5,
+                delta: float = 2.0) -> np.ndarray:
+    """Relative inlet excess J(y) in [0, 1] of a plane jet: 1 in the middle half of the
+    y-period, 0 outside, joined by tanh shear layers of width `delta` coarse cells; evaluated at
+    the cell centres of a grid `factor` times finer.  The inlet velocity is
+    u_in (1 + ratio J) (1 + noise)."""
+    fy = ny * factor
+    y = (np.arange(fy) + 0.5) / factor
+    j = 0.5 * (np.tanh((y - ny / 4) / delta) - np.tanh((y - 3 * ny / 4) / delta))
+    return ratio * np.tile(j[:, None], (1, nx * factor))
+
+
+def inlet_velocity(cx, cy, factor, u_in, noise_amp, jet_ratio, seed):
+    return (u_in * (1.0 + jet_profile(cx, cy, factor, jet_ratio)) *
+            (1.0 + noise_amp * inlet_noise(cx, cy, factor, seed=seed)))
 
 
 def channel(nx, ny, nz, u_in, re, length, lattice="D3Q19", cs=0.0, steps=1000):
@@ -144,14 +167,14 @@ def start_uniform(part, n, u_in):
 
 
 def run_fine(cx, cy, cz, factor, u_in, re, noise_amp, coarse_steps, snap_every, precision="f32",
-             device=0, seed=11):
-    """Fine BGK run; returns filtered snapshots keyed by coarse step."""
-    g, p = channel(cx * factor, cy * factor, cz * factor, u_in, re, cy * factor)
+             device=0, seed=11, fine_cs=0.05, jet_ratio=0.5):
+    """Fine run (BGK, or Smagorinsky with constant fine_cs); returns filtered snapshots keyed
+    by coarse step."""
+    g, p = channel(cx * factor, cy * factor, cz * factor, u_in, re, cy * factor, cs=fine_cs)
     part = TLBMPartition.from_arrays(problem_from_params(p), g.nd_type, precision=precision,
                                      arithmetic="fast", device=device)
     start_uniform(part, g.nx * g.ny * g.nz, u_in)
-    xi = inlet_noise(cx, cy, factor, seed=seed)
-    part.set_inlet_profile(u_in * (1.0 + noise_amp * xi))
+    part.set_inlet_profile(inlet_velocity(cx, cy, factor, u_in, noise_amp, jet_ratio, seed))
     snaps = {}
     ts = 0
     for k in range(snap_every, coarse_steps + 1, snap_every):
@@ -196,12 +219,12 @@ def train_closure(raw, targets, epochs=30, batch=8192, lr=2e-3, seed=5, device=0
 
 
 def run_coarse(cx, cy, cz, u_in, re, noise_amp, steps, closure=None, cs=0.0, precision="f32",
-               device=0, seed=11, tau_min=None):
+               device=0, seed=11, tau_min=None, jet_ratio=0.5):
     g, p = channel(cx, cy, cz, u_in, re, cy, cs=cs)
     part = TLBMPartition.from_arrays(problem_from_params(p), g.nd_type, precision=precision,
                                      arithmetic="fast", device=device)
     start_uniform(part, cx * cy * cz, u_in)
-    part.set_inlet_profile(u_in * (1.0 + noise_amp * inlet_noise(cx, cy, 1, seed=seed)))
+    part.set_inlet_profile(inlet_velocity(cx, cy, 1, u_in, noise_amp, jet_ratio, seed))
     nu = (1.0 / p.omega - 0.5) / 3.0
     if closure is not None:
         part.set_closure_mlp(closure["params"], closure["scale"], closure["shift"],
@@ -223,11 +246,12 @@ def evaluate(run, ref_uz, z_planes):
 
 
 def study(cx=128, cy=64, cz=64, factor=4, u_in=0.05, re=3000.0, noise_amp=0.01,
-          coarse_steps=1024, snap_every=64, train_from=512, epochs=30, device=0, seed=11):
+          coarse_steps=1024, snap_every=64, train_from=512, epochs=30, device=0, seed=11,
+          fine_cs=0.05, jet_ratio=0.5):
     """The learned-closure experiment; returns errors of Smagorinsky and the learned closure
     against the filtered fine run at `coarse_steps`, and their costs per step."""
     snaps, omega_f = run_fine(cx, cy, cz, factor, u_in, re, noise_amp, coarse_steps, snap_every,
-                              device=device, seed=seed)
+                              device=device, seed=seed, fine_cs=fine_cs, jet_ratio=jet_ratio)
     nu_c = u_in * cy / re
     train = {k: v for k, v in snaps.items() if train_from <= k < coarse_steps}
     raw, nut = build_dataset(train, nu_c, nu_cap=50.0 * nu_c)
@@ -240,6 +264,6 @@ def study(cx=128, cy=64, cz=64, factor=4, u_in=0.05, re=3000.0, noise_amp=0.01,
     for name, kw in (("smagorinsky", {"cs": 0.1}), ("learned", {"closure": cl}),
                      ("none", {})):
         r = run_coarse(cx, cy, cz, u_in, re, noise_amp, coarse_steps, device=device, seed=seed,
-                       **kw)
+                       jet_ratio=jet_ratio, **kw)
         out[name] = evaluate(r, ref, zp)
     return out, cl

@@ -252,6 +252,28 @@ tlbm_status tlbm_filtered_fields(tlbm_handle* h, int factor, void* out) {
   TLBM_CALL(h, h->engine->filtered(factor, out));
 }
 
+tlbm_status tlbm_processed_fields(tlbm_handle* h, int time_avg, float* out) {
+  if (!out) return TLBM_ERR_INVALID_ARGUMENT;
+  TLBM_CALL(h, h->engine->processed(time_avg != 0, out));
+}
+
+tlbm_status tlbm_write_processed_data(tlbm_handle* h, int time_avg) {
+  TLBM_CALL(h, h->engine->write_processed(time_avg != 0));
+}
+
+tlbm_status tlbm_process_output_dir(const char* workdir, int device, int* dumps) {
+  int done = 0;
+  try {
+    tlbm::Status s = tlbm::post_process_dir(workdir ? workdir : ".", device, &done);
+    if (dumps) *dumps = done;
+    if (!s.good()) return fail_create(s);
+    return TLBM_OK;
+  } catch (const std::bad_alloc&) {
+    if (dumps) *dumps = done;
+    return fail_create(tlbm::Status::err(TLBM_ERR_NO_MEMORY, "out of host memory"));
+  }
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------- ensembles

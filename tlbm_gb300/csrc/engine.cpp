@@ -24,6 +24,7 @@
 
 #include "mlp.cuh"
 #include "mlp_kernels.h"
+#include "post.h"
 
 namespace tlbm {
 
@@ -86,9 +87,11 @@ Status parse_params(const std::string& text, bool as_float, tlbm_problem* p) {
   int* dims[] = {&p->nx, &p->ny, &p->nz, &p->restart_flag, &p->time_avg_flag};
   for (int k = 0; k < 5; ++k) ok = ok && parse_token(tok[10 + k], dims[k]);
   if (!ok) return Status::err(TLBM_ERR_FORMAT, "params.lbm: malformed value in lines 2-15");
+  // the conversion factors only feed post-processing, which reads them as Python floats
+  // (python/processTLBM.py:42-47): always parsed in double
   double* phys[] = {&p->lx_p, &p->ly_p, &p->lz_p, &p->t_conv, &p->l_conv, &p->p_conv};
   for (int k = 0; k < 6 && 15 + k < (int)tok.size(); ++k)
-    if (!parse_real(tok[15 + k], as_float, phys[k]))
+    if (!parse_real(tok[15 + k], false, phys[k]))
       return Status::err(TLBM_ERR_FORMAT, "params.lbm: malformed value on line " +
                                               std::to_string(16 + k));
   if (tok.size() > 21 && !parse_token(tok[21], &p->p_ref_idx))
@@ -102,7 +105,9 @@ Status parse_int_file(const std::string& path, int64_t n, std::vector<int32_t>* 
   std::string text;
   Status s = read_text(path, &text);
   if (!s.good()) return s;
-  out->assign(static_cast<size_t>(n), 0);
+  const bool any = n < 0;
+  if (any) out->clear();
+  else out->assign(static_cast<size_t>(n), 0);
   const char* c = text.data();
   const char* end = c + text.size();
   int64_t k = 0;
@@ -126,12 +131,17 @@ Status parse_int_file(const std::string& path, int64_t n, std::vector<int32_t>* 
     if (c < end && !(*c == ' ' || *c == '\n' || *c == '\t' || *c == '\r'))
       return Status::err(TLBM_ERR_FORMAT, path + ": non-integer value at entry " +
                                               std::to_string(k));
+    if (any) {
+      out->push_back(static_cast<int32_t>(neg ? -v : v));
+      ++k;
+      continue;
+    }
     if (k >= n)
       return Status::err(TLBM_ERR_FORMAT, path + " has more than nx*ny*nz = " +
                                               std::to_string(n) + " values");
     (*out)[k++] = static_cast<int32_t>(neg ? -v : v);
   }
-  if (k != n)
+  if (!any && k != n)
     return Status::err(TLBM_ERR_FORMAT, path + " has " + std::to_string(k) +
                                             " values, expected nx*ny*nz = " + std::to_string(n));
   return Status::ok();
@@ -227,6 +237,8 @@ Engine::~Engine() {
   cudaFree(d_inlet_f_);
   cudaFree(d_closure_);
   cudaFree(d_closure_w_);
+  cudaFree(d_ss_);
+  cudaFree(d_ss_stage_);
   if (h_pinned_) cudaFreeHost(h_pinned_);
   if (stream_) cudaStreamDestroy(stream_);
 }
@@ -455,6 +467,44 @@ Status Engine::init(const int32_t* nd_type, const int32_t* parts, int size) {
     }
     TLBM_TRY(write_at(workdir_ + "/ordering.b_dat", op, n * sizeof(int32_t), 0));
   }
+  return load_subspace();
+}
+
+// Sub-space output: tLBM_write_params.py writes the subset node list to ssNds.lbm and the flag
+// to params.lbm line 23 (python/tLBM_write_params.py:110-117, :166); the reference reads the
+// flag (src/Problem.cpp:32) but never uses it.  Here each dump also writes ss_ux{n},
+// ss_uy{n}, ss_uz{n} and ss_density{n}.b_dat: the dump's values at the listed nodes, in list
+// order, gathered on the device.
+Status Engine::load_subspace() {
+  if (prob_.ss_data_flag != 1 || workdir_.empty()) return Status::ok();
+  TLBM_TRY(parse_int_file(workdir_ + "/ssNds.lbm", -1, &ss_));
+  for (size_t k = 0; k < ss_.size(); ++k)
+    if (ss_[k] < 0 || ss_[k] >= n_)
+      return Status::err(TLBM_ERR_OUT_OF_RANGE, "ssNds.lbm: entry " + std::to_string(k) +
+                                                    " is not a node of the lattice");
+  if (ss_.empty()) return Status::ok();
+  const size_t m = ss_.size();
+  TLBM_CUDA(cudaMalloc(&d_ss_, m * sizeof(int32_t)));
+  TLBM_CUDA(cudaMemcpy(d_ss_, ss_.data(), m * sizeof(int32_t), cudaMemcpyHostToDevice));
+  TLBM_CUDA(cudaMalloc(&d_ss_stage_, m * ob_));
+  return Status::ok();
+}
+
+Status Engine::write_subspace(const std::string& d) {
+  const size_t m = ss_.size();
+  std::vector<char> host(m * ob_);
+  const char* names[4] = {"ss_ux", "ss_uy", "ss_uz", "ss_density"};
+  for (int k = 0; k < 4; ++k) {
+    if (m) {
+      TLBM_CUDA(launch_gather(d_macro_[k], d_ss_, static_cast<int64_t>(m), ob_, d_ss_stage_,
+                              launch_));
+      ++launches_;
+      TLBM_CUDA(cudaMemcpyAsync(host.data(), d_ss_stage_, m * ob_, cudaMemcpyDeviceToHost,
+                                stream_));
+      TLBM_CUDA(cudaStreamSynchronize(stream_));
+    }
+    TLBM_TRY(write_at(workdir_ + "/" + names[k] + d + ".b_dat", host.data(), m * ob_, 0));
+  }
   return Status::ok();
 }
 
@@ -611,6 +661,7 @@ Status Engine::write_data() {
   TLBM_TRY(write_field("Fx" + d + ".b_dat", d_force_[0]));
   TLBM_TRY(write_field("Fy" + d + ".b_dat", d_force_[1]));
   TLBM_TRY(write_field("Fz" + d + ".b_dat", d_force_[2]));
+  if (prob_.ss_data_flag == 1) TLBM_TRY(write_subspace(d));
   ++dump_num_;
   return Status::ok();
 }
@@ -624,6 +675,60 @@ Status Engine::write_time_avg_data() {
   TLBM_TRY(write_field("vAvg.b_dat", d_avg_[1]));
   TLBM_TRY(write_field("wAvg.b_dat", d_avg_[2]));
   TLBM_TRY(write_field("rhoAvg.b_dat", d_avg_[3]));
+  return Status::ok();
+}
+
+Status Engine::processed(bool time_avg, float* out) {
+  TLBM_CUDA(cudaSetDevice(opt_.device));
+  if (prob_.p_ref_idx < 0 || prob_.p_ref_idx >= n_)
+    return Status::err(TLBM_ERR_OUT_OF_RANGE, "params.lbm: pRef_idx outside the lattice");
+  const void* f[7] = {};
+  if (time_avg) {
+    if (prob_.time_avg_flag != 1)
+      return Status::err(TLBM_ERR_INVALID_ARGUMENT, "time averaging is off (params.lbm line 15)");
+    for (int k = 0; k < 4; ++k) f[k] = d_avg_[k];
+  } else {
+    TLBM_TRY(compute_outputs());
+    for (int k = 0; k < 4; ++k) f[k] = d_macro_[k];
+    for (int k = 0; k < 3; ++k) f[4 + k] = d_force_[k];
+  }
+  const size_t planes = time_avg ? kPostAvgFields : kPostFields;
+  const size_t bytes = static_cast<size_t>(n_) * 4 * planes;
+  float* d = nullptr;
+  TLBM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d), bytes, stream_));
+  const PostFactors k = post_factors(prob_, time_avg);
+  cudaError_t e;
+  if (ob_ == 4) {
+    PostInputs<float> in;
+    const float** p[7] = {&in.ux, &in.uy, &in.uz, &in.rho, &in.fx, &in.fy, &in.fz};
+    for (int i = 0; i < 7; ++i) *p[i] = static_cast<const float*>(f[i]);
+    e = launch_post(in, nullptr, n_, prob_.p_ref_idx, k, d, stream_);
+  } else {
+    PostInputs<double> in;
+    const double** p[7] = {&in.ux, &in.uy, &in.uz, &in.rho, &in.fx, &in.fy, &in.fz};
+    for (int i = 0; i < 7; ++i) *p[i] = static_cast<const double*>(f[i]);
+    e = launch_post(in, nullptr, n_, prob_.p_ref_idx, k, d, stream_);
+  }
+  ++launches_;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, bytes, cudaMemcpyDeviceToHost, stream_);
+  cudaFreeAsync(d, stream_);
+  TLBM_CUDA(e);
+  TLBM_CUDA(cudaStreamSynchronize(stream_));
+  return Status::ok();
+}
+
+Status Engine::write_processed(bool time_avg) {
+  if (workdir_.empty()) return Status::err(TLBM_ERR_IO, "no output directory");
+  std::vector<float> host(static_cast<size_t>(n_) * (time_avg ? kPostAvgFields : kPostFields));
+  TLBM_TRY(processed(time_avg, host.data()));
+  const std::string d = std::to_string(proc_num_);
+  std::string err;
+  const bool ok = time_avg ? post_write(workdir_, "timeAvg.bin", "timeAvg.xmf", prob_,
+                                        host.data(), true, &err)
+                           : post_write(workdir_, "out" + d + ".bin", "data" + d + ".xmf", prob_,
+                                        host.data(), false, &err);
+  if (!ok) return Status::err(TLBM_ERR_IO, err);
+  if (!time_avg) ++proc_num_;
   return Status::ok();
 }
 

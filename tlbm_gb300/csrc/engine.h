@@ -28,10 +28,12 @@ struct Status {
 // Problem::load_input semantics (src/Problem.cpp:5-32): 23 whitespace-separated tokens.
 // Real values are parsed in the precision that will compute with them.
 Status parse_params(const std::string& text, bool as_float, tlbm_problem* p);
-// whitespace-separated integers of ndType.lbm / parts.lbm, exactly n of them
+// whitespace-separated integers of ndType.lbm / parts.lbm, exactly n of them (n < 0: any count)
 Status parse_int_file(const std::string& path, int64_t n, std::vector<int32_t>* out);
 Status read_text(const std::string& path, std::string* out);
 Status apply_config_file(const std::string& path, tlbm_options* opt);
+// processTLBM.py over a run directory (post.cpp): dumps 0 .. nDumps-1 and the time averages
+Status post_process_dir(const std::string& dir, int device, int* dumps_done);
 
 class Engine {
  public:
@@ -60,6 +62,10 @@ class Engine {
                      float out_scale, float tau_min);
   // box filter by f of the last step's macroscopic fields: 10 coarse fields (mlp_kernels.h)
   Status filtered(int f, void* out);
+  // processTLBM.py's fields of the last step (or of the time averages), planes of post.h
+  Status processed(bool time_avg, float* out);
+  // ... written as out{k}.bin + data{k}.xmf (k = 0, 1, ... per call) or timeAvg.bin/.xmf
+  Status write_processed(bool time_avg);
 
   const tlbm_problem& problem() const { return prob_; }
   int output_bytes() const { return ob_; }
@@ -113,7 +119,15 @@ class Engine {
   void* d_closure_ = nullptr;    // mlp::Closure
   float* d_closure_w_ = nullptr;  // its weights
 
+  // sub-space output (params.lbm line 23, ssNds.lbm): node list and gathered values
+  std::vector<int32_t> ss_;
+  int32_t* d_ss_ = nullptr;
+  void* d_ss_stage_ = nullptr;
+  Status load_subspace();
+  Status write_subspace(const std::string& d);
+
   int last_src_ = -1, last_dst_ = -1;
+  int proc_num_ = 0;
   bool outputs_fresh_ = false;
   int dump_num_ = 0;
   int64_t steps_ = 0;

@@ -19,19 +19,60 @@ __global__ void __launch_bounds__(128) k_step_fast(StepArgs a) {
   cell_step<L, K, kClosure>(a, x, y, z);
 }
 
-// learned closure: the network's weights are staged in shared memory once per block
+// learned closure: the network runs on the tensor cores, one warp (32 cells) at a time
+// (mlp::forward_warp).  Non-fluid nodes finish before the network is evaluated; every lane
+// of a warp reaches the warp-collective part, which a warp without fluid cells skips.
 template <class L, int K>
 __global__ void __launch_bounds__(128) k_step_fast_mlp(StepArgs a) {
-  __shared__ float sw[mlp::kParams];
+  using S = Store<K>;
+  using C = typename S::C;
+  __shared__ mlp::MmaWeights sw;
+  __shared__ uint4 xs[4][32];
+  __shared__ float ys[4][32];
   const mlp::Closure* cl = static_cast<const mlp::Closure*>(a.closure);
   const int tid = threadIdx.x + threadIdx.y * blockDim.x;
-  for (int k = tid; k < mlp::kParams; k += blockDim.x * blockDim.y) sw[k] = cl->w[k];
+  mlp::stage_mma_weights(cl->w, sw, tid, blockDim.x * blockDim.y);
   __syncthreads();
+  const DevProblem& pb = a.pb;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
-  if (x >= a.pb.nx || y >= a.pb.ny) return;
-  cell_step<L, K, fast::kClosureMlp>(a, x, y, z, sw);
+  const bool in = x < pb.nx && y < pb.ny;
+  const int c = x + y * pb.nx + z * pb.nxy;
+  bool fluid = false;
+  C f[L::Q];
+  fast::FluidPre<L, C> st;
+  float xin[mlp::kIn] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if (in) {
+    typename S::T raw[L::Q];
+    load_raw<L, K>(a, x, y, z, c, raw);
+    const uint8_t t = pb.nd_type[c];
+    if (t == kFluid) {
+      fluid = true;
+      unpack<L, K>(raw, f);
+      fast::fluid_pre<L, C, true>(f, st);
+      if (pb.dynamics == 1) fast::closure_inputs<L, C>(st, cl, xin);
+    } else {
+      C rho = 0, ux = 0, uy = 0, uz = 0;
+      if (pb.cs > 0)
+        boundary_node<L, K, true>(a, x, y, c, t, raw, rho, ux, uy, uz);
+      else
+        boundary_node<L, K, false>(a, x, y, c, t, raw, rho, ux, uy, uz);
+      if (a.time_avg) accumulate_avg<C>(a, c, rho, ux, uy, uz);
+    }
+  }
+  const int warp = tid >> 5, lane = tid & 31;
+  float net = 0.f;
+  if (__any_sync(0xFFFFFFFFu, fluid && pb.dynamics == 1))
+    net = mlp::forward_warp(sw, xs[warp], ys[warp], xin, lane);
+  if (!fluid) return;
+  if (pb.dynamics == 1) {
+    const C omega = fast::closure_omega<C>(net, cl, Par<C>::omega(pb), Par<C>::cs(pb),
+                                           Par<C>::nu(pb), st.q2);
+    fast::fluid_relax<L, C>(f, st, omega);
+  }
+  store_cell<L, K>(a, c, f);
+  if (a.time_avg) accumulate_avg<C>(a, c, st.rho, st.ux, st.uy, st.uz);
 }
 
 template <class L, int K>

@@ -186,18 +186,25 @@ __global__ void k_mlp_round(const float* __restrict__ w, float* __restrict__ wbf
   if (p < kParams) wbf[p] = is_bias(p) ? w[p] : bf16r(w[p]);
 }
 
+// Inference exactly as the collide kernel runs it: the tensor-core forward pass of mlp.cuh,
+// 32 samples per warp.
 __global__ void __launch_bounds__(kTile) k_mlp_predict(const float* __restrict__ wbf,
                                                        const float* __restrict__ feats, int64_t n,
                                                        float* __restrict__ y) {
-  __shared__ float sw[kParams];
-  for (int k = threadIdx.x; k < kParams; k += kTile) sw[k] = wbf[k];
+  __shared__ MmaWeights sw;
+  __shared__ uint4 xs[kTile / 32][32];
+  __shared__ float ys[kTile / 32][32];
+  stage_mma_weights(wbf, sw, threadIdx.x, kTile);
   __syncthreads();
-  for (int64_t i = blockIdx.x * static_cast<int64_t>(kTile) + threadIdx.x; i < n;
-       i += static_cast<int64_t>(gridDim.x) * kTile) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int64_t base = blockIdx.x * static_cast<int64_t>(kTile) + warp * 32; base < n;
+       base += static_cast<int64_t>(gridDim.x) * kTile) {
+    const int64_t i = base + lane;
     float x[kIn];
 #pragma unroll
-    for (int k = 0; k < kIn; ++k) x[k] = feats[i * kIn + k];
-    y[i] = forward(sw, x);
+    for (int k = 0; k < kIn; ++k) x[k] = i < n ? feats[i * kIn + k] : 0.0f;
+    const float v = forward_warp(sw, xs[warp], ys[warp], x, lane);
+    if (i < n) y[i] = v;
   }
 }
 

@@ -53,21 +53,13 @@ __device__ __forceinline__ void node_macros(uint8_t t, const C (&f)[L::Q], C u_b
   }
 }
 
-// kClosure: fast::kClosureNone (BGK), kClosureSmag, kClosureMlp (sw = the closure's weights
-// in shared memory; boundary nodes then use Smagorinsky when cs > 0)
-template <class L, int K, int kClosure>
-__device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z,
-                                          const float* sw = nullptr) {
-  using S = Store<K>;
-  using C = typename S::C;
-  using T = typename S::T;
+// the Q stored values cell c pulls (from c - e_i, periodic)
+template <class L, int K>
+__device__ __forceinline__ void load_raw(const StepArgs& a, int x, int y, int z, int c,
+                                         typename Store<K>::T (&raw)[L::Q]) {
+  using T = typename Store<K>::T;
   const DevProblem& pb = a.pb;
-  const int c = x + y * pb.nx + z * pb.nxy;
-  const size_t n = static_cast<size_t>(pb.n);
   const T* __restrict__ src = static_cast<const T*>(a.src);
-  T* __restrict__ dst = static_cast<T*>(a.dst);
-
-  T raw[L::Q];
   if (x > 0 && x < pb.nx - 1 && y > 0 && y < pb.ny - 1 && z > 0 && z < pb.nz - 1) {
     // interior cell: speed i comes from a fixed byte offset of the cell's own slot
     const char* base = reinterpret_cast<const char*>(src + c);
@@ -76,8 +68,107 @@ __device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z
       raw[i] = __ldg(reinterpret_cast<const T*>(base + pb.pull_off[i]));
   } else {
     const Nbr nb(x, y, z, pb.nx, pb.ny, pb.nz, pb.nxy);
-    load_cell<L, K>(src, n, nb, raw);
+    load_cell<L, K>(src, static_cast<size_t>(pb.n), nb, raw);
   }
+}
+
+template <class L, int K>
+__device__ __forceinline__ void store_cell(const StepArgs& a, int c,
+                                           const typename Store<K>::C (&f)[L::Q]) {
+  using S = Store<K>;
+  using C = typename S::C;
+  typename S::T* __restrict__ dst = static_cast<typename S::T*>(a.dst);
+  const size_t n = static_cast<size_t>(a.pb.n);
+#pragma unroll
+  for (int i = 0; i < L::Q; ++i) dst[i * n + c] = S::save(f[i], fast::wgt<L, C>(i));
+}
+
+// every node type but fluid: solid bounce-back, inlet/outlet reconstruction and relaxation,
+// the moving-wall nudge.  kSmag: boundary nodes relax at the Smagorinsky rate.
+template <class L, int K, bool kSmag>
+__device__ __forceinline__ void boundary_node(const StepArgs& a, int x, int y, int c, uint8_t t,
+                                              const typename Store<K>::T (&raw)[L::Q],
+                                              typename Store<K>::C& rho,
+                                              typename Store<K>::C& ux,
+                                              typename Store<K>::C& uy,
+                                              typename Store<K>::C& uz) {
+  using S = Store<K>;
+  using C = typename S::C;
+  const DevProblem& pb = a.pb;
+  if (t == kSolid) {
+    typename S::T* __restrict__ dst = static_cast<typename S::T*>(a.dst);
+    const size_t n = static_cast<size_t>(pb.n);
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) dst[i * n + c] = raw[L::bb(i)];
+    if (a.time_avg) {
+      C f[L::Q];
+      unpack<L, K>(raw, f);
+      rho = fast::density<L, C>(f);
+    }
+    return;
+  }
+  C f[L::Q];
+  unpack<L, K>(raw, f);
+  const C u_bc = (t == kInlet) ? Par<C>::u_in(pb, x + y * pb.nx) : Par<C>::u_bc(pb);
+  node_macros<L, C>(t, f, u_bc, Par<C>::rho_bc(pb), rho, ux, uy, uz);
+  if constexpr (S::kShifted) {
+    // 16-bit storage: the inlet density and outlet velocity sums are taken in FP64
+    if (t == kInlet || t == kOutlet) {
+      double fd[L::Q];
+#pragma unroll
+      for (int i = 0; i < L::Q; ++i)
+        fd[i] = static_cast<double>(fast::wgt<L, float>(i)) +
+                static_cast<double>(S::load(raw[i], 0.0f));
+      if (t == kInlet)
+        rho = static_cast<C>(fast::inlet_rho<L, double>(
+            fd, 1.0 / (1.0 - Par<double>::u_in(pb, x + y * pb.nx))));
+      else
+        uz = static_cast<C>(fast::outlet_uz<L, double>(fd, 1.0 / pb.rho_bc));
+    }
+  }
+  if (pb.has_type5 && t == kMovingWall) {
+    const C* cur = static_cast<const C*>(a.uyq_cur);
+    const C* prev = static_cast<const C*>(a.uyq_prev);
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) {
+      const C uyq = i <= c ? cur[i] : prev[i];
+      f[i] += C(3) * rho * fast::wgt<L, C>(i) *
+              (C(L::ez(i)) * (u_bc - uz) - C(L::ex(i)) * ux - C(L::ey(i)) * uyq);
+    }
+  }
+  C feq[L::Q];
+  fast::equilibrium<L, C>(rho, ux, uy, uz, feq);
+  if (t == kInlet) fast::nebb<L, C, true>(f, feq);
+  if (t == kOutlet) fast::nebb<L, C, false>(f, feq);
+  if (pb.dynamics == 1) {
+    C om = Par<C>::omega(pb);
+    if (kSmag) om = fast::smagorinsky_omega<L, C>(f, feq, Par<C>::cs(pb), Par<C>::nu(pb));
+    fast::relax<L, C>(f, feq, om);
+  }
+  store_cell<L, K>(a, c, f);
+}
+
+template <class C>
+__device__ __forceinline__ void accumulate_avg(const StepArgs& a, int c, C rho, C ux, C uy,
+                                               C uz) {
+  C* const* avg = reinterpret_cast<C* const*>(a.avg);
+  avg[0][c] += ux;
+  avg[1][c] += uy;
+  avg[2][c] += uz;
+  avg[3][c] += rho;
+}
+
+// kClosure: fast::kClosureNone (BGK), kClosureSmag, kClosureMlp (sw = the closure's weights
+// in shared memory; boundary nodes then use Smagorinsky when cs > 0)
+template <class L, int K, int kClosure>
+__device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z,
+                                          const float* sw = nullptr) {
+  using S = Store<K>;
+  using C = typename S::C;
+  const DevProblem& pb = a.pb;
+  const int c = x + y * pb.nx + z * pb.nxy;
+  typename S::T raw[L::Q];
+  load_raw<L, K>(a, x, y, z, c, raw);
   const uint8_t t = pb.nd_type[c];
   C rho = 0, ux = 0, uy = 0, uz = 0;
   if (t == kFluid) {
@@ -86,66 +177,13 @@ __device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z
     fast::fluid_collide<L, C, kClosure>(f, Par<C>::omega(pb), Par<C>::cs(pb), Par<C>::nu(pb),
                                         pb.dynamics == 1, rho, ux, uy, uz,
                                         static_cast<const mlp::Closure*>(a.closure), sw);
-#pragma unroll
-    for (int i = 0; i < L::Q; ++i) dst[i * n + c] = S::save(f[i], fast::wgt<L, C>(i));
-  } else if (t == kSolid) {
-#pragma unroll
-    for (int i = 0; i < L::Q; ++i) dst[i * n + c] = raw[L::bb(i)];
-    if (a.time_avg) {
-      C f[L::Q];
-      unpack<L, K>(raw, f);
-      rho = fast::density<L, C>(f);
-    }
+    store_cell<L, K>(a, c, f);
+  } else if (kClosure == fast::kClosureSmag || (kClosure == fast::kClosureMlp && pb.cs > 0)) {
+    boundary_node<L, K, true>(a, x, y, c, t, raw, rho, ux, uy, uz);
   } else {
-    C f[L::Q];
-    unpack<L, K>(raw, f);
-    const C u_bc = (t == kInlet) ? Par<C>::u_in(pb, x + y * pb.nx) : Par<C>::u_bc(pb);
-    node_macros<L, C>(t, f, u_bc, Par<C>::rho_bc(pb), rho, ux, uy, uz);
-    if constexpr (S::kShifted) {
-      // 16-bit storage: the inlet density and outlet velocity sums are taken in FP64
-      if (t == kInlet || t == kOutlet) {
-        double fd[L::Q];
-#pragma unroll
-        for (int i = 0; i < L::Q; ++i)
-          fd[i] = static_cast<double>(fast::wgt<L, float>(i)) +
-                  static_cast<double>(S::load(raw[i], 0.0f));
-        if (t == kInlet)
-          rho = static_cast<C>(fast::inlet_rho<L, double>(
-              fd, 1.0 / (1.0 - Par<double>::u_in(pb, x + y * pb.nx))));
-        else
-          uz = static_cast<C>(fast::outlet_uz<L, double>(fd, 1.0 / pb.rho_bc));
-      }
-    }
-    if (pb.has_type5 && t == kMovingWall) {
-      const C* cur = static_cast<const C*>(a.uyq_cur);
-      const C* prev = static_cast<const C*>(a.uyq_prev);
-#pragma unroll
-      for (int i = 0; i < L::Q; ++i) {
-        const C uyq = i <= c ? cur[i] : prev[i];
-        f[i] += C(3) * rho * fast::wgt<L, C>(i) *
-                (C(L::ez(i)) * (u_bc - uz) - C(L::ex(i)) * ux - C(L::ey(i)) * uyq);
-      }
-    }
-    C feq[L::Q];
-    fast::equilibrium<L, C>(rho, ux, uy, uz, feq);
-    if (t == kInlet) fast::nebb<L, C, true>(f, feq);
-    if (t == kOutlet) fast::nebb<L, C, false>(f, feq);
-    if (pb.dynamics == 1) {
-      C om = Par<C>::omega(pb);
-      if (kClosure == fast::kClosureSmag || (kClosure == fast::kClosureMlp && pb.cs > 0))
-        om = fast::smagorinsky_omega<L, C>(f, feq, Par<C>::cs(pb), Par<C>::nu(pb));
-      fast::relax<L, C>(f, feq, om);
-    }
-#pragma unroll
-    for (int i = 0; i < L::Q; ++i) dst[i * n + c] = S::save(f[i], fast::wgt<L, C>(i));
+    boundary_node<L, K, false>(a, x, y, c, t, raw, rho, ux, uy, uz);
   }
-  if (a.time_avg) {
-    C* const* avg = reinterpret_cast<C* const*>(a.avg);
-    avg[0][c] += ux;
-    avg[1][c] += uy;
-    avg[2][c] += uz;
-    avg[3][c] += rho;
-  }
+  if (a.time_avg) accumulate_avg<C>(a, c, rho, ux, uy, uz);
 }
 
 }  // namespace tlbm
