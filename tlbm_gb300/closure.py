@@ -229,7 +229,7 @@ def run_coarse(cx, cy, cz, u_in, re, noise_amp, steps, closure=None, cs=0.0, pre
     if closure is not None:
         part.set_closure_mlp(closure["params"], closure["scale"], closure["shift"],
                              closure["out_scale"], tau_min if tau_min else 3.0 * nu + 0.5 + 1e-6)
-    ms = part.time_steps(0, steps)
+    ms = part.time_steps(0, steps) / steps
     ux, uy, uz, rho = part.macros()
     part.close()
     return {"uz": uz.reshape(cz, cy, cx), "ms": ms, "finite": bool(np.isfinite(uz).all()),

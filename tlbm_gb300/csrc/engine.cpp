@@ -235,7 +235,7 @@ Engine::~Engine() {
   cudaFree(d_mass_);
   cudaFree(d_inlet_d_);
   cudaFree(d_inlet_f_);
-  cudaFree(d_closure_);
+  delete static_cast<mlp::Closure*>(h_closure_);
   cudaFree(d_closure_w_);
   cudaFree(d_ss_);
   cudaFree(d_ss_stage_);
@@ -529,7 +529,7 @@ Status Engine::enqueue_step(int is_even) {
     }
     TLBM_CUDA(launch_step_ref(q_, sb_, a, launch_));
   } else {
-    a.closure = d_closure_;
+    a.closure = h_closure_;
     TLBM_CUDA(launch_step_fast(q_, store_, a, launch_));
     if (has_type5_) ++launches_;
   }
@@ -863,33 +863,29 @@ Status Engine::set_closure(const float* params, const float* scale, const float*
   TLBM_CUDA(cudaStreamSynchronize(stream_));
   drop_graphs();
   if (!params) {
-    cudaFree(d_closure_);
-    d_closure_ = nullptr;
+    delete static_cast<mlp::Closure*>(h_closure_);
+    h_closure_ = nullptr;
     return Status::ok();
   }
   if (!scale || !shift || !(tau_min > 0.5f) || !std::isfinite(out_scale))
     return Status::err(TLBM_ERR_INVALID_ARGUMENT,
                        "closure needs 8 scales and shifts, a finite out_scale and tau_min > 1/2");
-  // weights rounded to BF16 once here; biases stay FP32 (mlp.cuh)
-  std::vector<float> w(params, params + mlp::kParams);
-  for (int p = 0; p < mlp::kParams; ++p) {
-    const bool bias = (p >= mlp::oB1 && p < mlp::oW2) || (p >= mlp::oB2 && p < mlp::oW3) ||
-                      p == mlp::oB3;
-    if (!bias) w[p] = mlp::bf16r(w[p]);
-  }
-  if (!d_closure_w_) TLBM_CUDA(cudaMalloc(&d_closure_w_, mlp::kParams * sizeof(float)));
-  TLBM_CUDA(cudaMemcpy(d_closure_w_, w.data(), mlp::kParams * sizeof(float),
-                       cudaMemcpyHostToDevice));
+  // the tensor-core image: weights rounded to BF16 once here, biases FP32 (mlp.cuh)
+  mlp::MmaWeights img;
+  mlp::build_mma_weights(params, &img);
+  if (!d_closure_w_) TLBM_CUDA(cudaMalloc(&d_closure_w_, sizeof(mlp::MmaWeights)));
+  TLBM_CUDA(cudaMemcpy(d_closure_w_, &img, sizeof(img), cudaMemcpyHostToDevice));
   mlp::Closure c{};
-  c.w = d_closure_w_;
+  c.w = static_cast<const mlp::MmaWeights*>(d_closure_w_);
   for (int k = 0; k < mlp::kIn; ++k) {
     c.scale[k] = scale[k];
     c.shift[k] = shift[k];
+    c.offset[k] = -shift[k] * scale[k];
   }
   c.out_scale = out_scale;
   c.tau_min = tau_min;
-  if (!d_closure_) TLBM_CUDA(cudaMalloc(&d_closure_, sizeof(mlp::Closure)));
-  TLBM_CUDA(cudaMemcpy(d_closure_, &c, sizeof(c), cudaMemcpyHostToDevice));
+  if (!h_closure_) h_closure_ = new mlp::Closure();
+  *static_cast<mlp::Closure*>(h_closure_) = c;
   return Status::ok();
 }
 

@@ -116,8 +116,8 @@ class Engine {
   void drop_graphs();
   double* d_inlet_d_ = nullptr;
   float* d_inlet_f_ = nullptr;
-  void* d_closure_ = nullptr;    // mlp::Closure
-  float* d_closure_w_ = nullptr;  // its weights
+  void* h_closure_ = nullptr;    // mlp::Closure (host: launches copy it by value)
+  void* d_closure_w_ = nullptr;   // its weights (mlp::MmaWeights)
 
   // sub-space output (params.lbm line 23, ssNds.lbm): node list and gathered values
   std::vector<int32_t> ss_;

@@ -19,20 +19,33 @@ __global__ void __launch_bounds__(128) k_step_fast(StepArgs a) {
   cell_step<L, K, kClosure>(a, x, y, z);
 }
 
-// learned closure: the network runs on the tensor cores, one warp (32 cells) at a time
-// (mlp::forward_warp).  Non-fluid nodes finish before the network is evaluated; every lane
-// of a warp reaches the warp-collective part, which a warp without fluid cells skips.
+// an opaque copy: the compiler cannot reuse values computed from v before this point
+__device__ __forceinline__ void launder(float& v) { asm volatile("" : "+f"(v)); }
+__device__ __forceinline__ void launder(double& v) { asm volatile("" : "+d"(v)); }
+
+// Learned closure.  The network runs on the tensor cores, one warp (32 cells) at a time
+// (mlp::forward_warp); the closure's description arrives by value in the kernel parameters.
+// The block starts the copy of the network to shared memory, loads and prepares its cells
+// (non-fluid nodes finish here), and only then waits for the copy, so the copy's latency hides
+// behind the cell loads.  Every lane of a warp reaches the warp-collective part, which a warp
+// without fluid cells skips.  Across the network only f, rho, u and Pi:Pi stay live; the pair
+// terms of the equilibrium are recomputed after it.
+#ifndef TLBM_MLP_MIN_BLOCKS
+#define TLBM_MLP_MIN_BLOCKS 8  // resident blocks per SM: 64 registers per thread
+#endif
+template <int K>
+constexpr int kMlpMinBlocks = K == kStoreF64 ? 4 : TLBM_MLP_MIN_BLOCKS;
+
 template <class L, int K>
-__global__ void __launch_bounds__(128) k_step_fast_mlp(StepArgs a) {
+__global__ void __launch_bounds__(128, kMlpMinBlocks<K>)
+    k_step_fast_mlp(StepArgs a, const mlp::Closure cl) {
   using S = Store<K>;
   using C = typename S::C;
   __shared__ mlp::MmaWeights sw;
   __shared__ uint4 xs[4][32];
   __shared__ float ys[4][32];
-  const mlp::Closure* cl = static_cast<const mlp::Closure*>(a.closure);
   const int tid = threadIdx.x + threadIdx.y * blockDim.x;
-  mlp::stage_mma_weights(cl->w, sw, tid, blockDim.x * blockDim.y);
-  __syncthreads();
+  mlp::copy_mma_weights(cl.w, sw, tid, blockDim.x * blockDim.y);
   const DevProblem& pb = a.pb;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -41,7 +54,7 @@ __global__ void __launch_bounds__(128) k_step_fast_mlp(StepArgs a) {
   const int c = x + y * pb.nx + z * pb.nxy;
   bool fluid = false;
   C f[L::Q];
-  fast::FluidPre<L, C> st;
+  C rho = 0, ux = 0, uy = 0, uz = 0, q2 = 0;
   float xin[mlp::kIn] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   if (in) {
     typename S::T raw[L::Q];
@@ -50,10 +63,15 @@ __global__ void __launch_bounds__(128) k_step_fast_mlp(StepArgs a) {
     if (t == kFluid) {
       fluid = true;
       unpack<L, K>(raw, f);
+      fast::FluidPre<L, C> st;
       fast::fluid_pre<L, C, true>(f, st);
+      rho = st.rho;
+      ux = st.ux;
+      uy = st.uy;
+      uz = st.uz;
+      q2 = st.q2;
       if (pb.dynamics == 1) fast::closure_inputs<L, C>(st, cl, xin);
     } else {
-      C rho = 0, ux = 0, uy = 0, uz = 0;
       if (pb.cs > 0)
         boundary_node<L, K, true>(a, x, y, c, t, raw, rho, ux, uy, uz);
       else
@@ -61,18 +79,28 @@ __global__ void __launch_bounds__(128) k_step_fast_mlp(StepArgs a) {
       if (a.time_avg) accumulate_avg<C>(a, c, rho, ux, uy, uz);
     }
   }
+  __syncthreads();  // the network is in shared memory
   const int warp = tid >> 5, lane = tid & 31;
   float net = 0.f;
   if (__any_sync(0xFFFFFFFFu, fluid && pb.dynamics == 1))
     net = mlp::forward_warp(sw, xs[warp], ys[warp], xin, lane);
   if (!fluid) return;
   if (pb.dynamics == 1) {
+    launder(ux);
+    launder(uy);
+    launder(uz);
+    fast::FluidPre<L, C> st;
+    st.rho = rho;
+    st.ux = ux;
+    st.uy = uy;
+    st.uz = uz;
+    fast::fluid_pair_terms<L, C>(st);
     const C omega = fast::closure_omega<C>(net, cl, Par<C>::omega(pb), Par<C>::cs(pb),
-                                           Par<C>::nu(pb), st.q2);
+                                           Par<C>::nu(pb), q2);
     fast::fluid_relax<L, C>(f, st, omega);
   }
   store_cell<L, K>(a, c, f);
-  if (a.time_avg) accumulate_avg<C>(a, c, st.rho, st.ux, st.uy, st.uz);
+  if (a.time_avg) accumulate_avg<C>(a, c, rho, ux, uy, uz);
 }
 
 template <class L, int K>
@@ -167,7 +195,7 @@ template <class L, int K>
 cudaError_t step_lk(const StepArgs& a, const Launch& l) {
   const dim3 g = grid_of(a.pb, l), b(l.bx, l.by, 1);
   if (a.closure)
-    k_step_fast_mlp<L, K><<<g, b, 0, l.stream>>>(a);
+    k_step_fast_mlp<L, K><<<g, b, 0, l.stream>>>(a, *static_cast<const mlp::Closure*>(a.closure));
   else if (a.pb.cs > 0)
     k_step_fast<L, K, fast::kClosureSmag><<<g, b, 0, l.stream>>>(a);
   else

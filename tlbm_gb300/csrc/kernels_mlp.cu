@@ -4,8 +4,8 @@
 // Training is deterministic: each block accumulates the gradient of its samples into
 // registers (one thread per group of parameters, samples staged in shared memory), writes one
 // partial per block, and a second kernel folds the partials in a fixed order.  Forward and
-// backward use the rounding of mlp::forward (BF16 weights and layer inputs, FP32
-// accumulation), so the gradient is the gradient of the network the collide kernel runs.
+// backward use the network of mlp.cuh (BF16 weights, BF16 act outputs, FP32 accumulation), so
+// the gradient is the gradient of the network the collide kernel runs.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -46,7 +46,7 @@ __device__ float sample_fb(Smem& s, int r, const float* __restrict__ xin, float 
     float z = w[oB1 + j];
 #pragma unroll
     for (int k = 0; k < kIn; ++k) z = fmaf(w[oW1 + j * kIn + k], x[k], z);
-    h1[j] = bf16r(tanh_fast(z));
+    h1[j] = act(z);
     s.h1[r][j] = h1[j];
   }
   float h2[kHid];
@@ -56,7 +56,7 @@ __device__ float sample_fb(Smem& s, int r, const float* __restrict__ xin, float 
     float z = w[oB2 + j];
 #pragma unroll
     for (int k = 0; k < kHid; ++k) z = fmaf(w[oW2 + j * kHid + k], h1[k], z);
-    h2[j] = bf16r(tanh_fast(z));
+    h2[j] = act(z);
     s.h2[r][j] = h2[j];
     y = fmaf(w[oW3 + j], h2[j], y);
   }

@@ -158,11 +158,10 @@ __device__ __forceinline__ void accumulate_avg(const StepArgs& a, int c, C rho, 
   avg[3][c] += rho;
 }
 
-// kClosure: fast::kClosureNone (BGK), kClosureSmag, kClosureMlp (sw = the closure's weights
-// in shared memory; boundary nodes then use Smagorinsky when cs > 0)
+// kClosure: fast::kClosureNone (BGK) or kClosureSmag (the learned closure has its own kernel,
+// kernels_fast.cu: k_step_fast_mlp)
 template <class L, int K, int kClosure>
-__device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z,
-                                          const float* sw = nullptr) {
+__device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z) {
   using S = Store<K>;
   using C = typename S::C;
   const DevProblem& pb = a.pb;
@@ -175,10 +174,9 @@ __device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z
     C f[L::Q];
     unpack<L, K>(raw, f);
     fast::fluid_collide<L, C, kClosure>(f, Par<C>::omega(pb), Par<C>::cs(pb), Par<C>::nu(pb),
-                                        pb.dynamics == 1, rho, ux, uy, uz,
-                                        static_cast<const mlp::Closure*>(a.closure), sw);
+                                        pb.dynamics == 1, rho, ux, uy, uz);
     store_cell<L, K>(a, c, f);
-  } else if (kClosure == fast::kClosureSmag || (kClosure == fast::kClosureMlp && pb.cs > 0)) {
+  } else if (kClosure == fast::kClosureSmag) {
     boundary_node<L, K, true>(a, x, y, c, t, raw, rho, ux, uy, uz);
   } else {
     boundary_node<L, K, false>(a, x, y, c, t, raw, rho, ux, uy, uz);
