@@ -71,13 +71,17 @@ typedef struct tlbm_options {
   int block_x;     /* threads per block along x; 0 = tuned by the engine */
   int block_y;     /* threads per block along y; 0 = tuned by the engine */
   int device;      /* CUDA device ordinal */
-  int reserved[9];
+  int rbgk;        /* 1: params.lbm dynamics 2 ("RBGK", include/Problem.h:19) runs the
+                      regularised BGK collision (fast arithmetic only); 0: the reference's
+                      behaviour, streaming without relaxation */
+  int reserved[8];
 } tlbm_options;
 
 /* The 23 values of params.lbm in file order (Problem, include/Problem.h:18-40). */
 typedef struct tlbm_problem {
   char lattice[8]; /* "D3Q15" | "D3Q19" | "D3Q27" */
-  int dynamics;    /* 1 = LBGK, 2 = stream without relaxation (reference behaviour) */
+  int dynamics;    /* 1 = LBGK, 2 = stream without relaxation (reference behaviour) or, with
+                      tlbm_options.rbgk, regularised BGK */
   int num_ts, ts_rep_freq, warmup_ts, plot_freq;
   double cs, rho_lbm, u_lbm, omega;
   int nx, ny, nz;
@@ -97,7 +101,7 @@ void tlbm_default_options(tlbm_options* opt);
  * process drives the whole lattice); `size` must exceed the largest partition id, as the
  * reference requires (src/TLBM_Partition.cpp:218-224).  Options: defaults, overridden by an
  * optional `tlbm.cfg` in workdir (lines `key value`: precision f64|f32|bf16|f16,
- * arithmetic reference|fast, block_x N, block_y N, device N). */
+ * arithmetic reference|fast, block_x N, block_y N, device N, rbgk 0|1). */
 tlbm_status tlbm_create(const char* workdir, int rank, int size, tlbm_handle** out);
 
 /* As tlbm_create with explicit options (tlbm.cfg is not read). */
@@ -227,12 +231,15 @@ tlbm_status tlbm_process_output_dir(const char* workdir, int device, int* dumps)
  * restores the uniform uLBM).  Used for seeded inlet perturbations. */
 tlbm_status tlbm_set_inlet_profile(tlbm_handle* h, const double* uz);
 
-/* Learned eddy-viscosity closure for fluid nodes: an 8-32-32-1 tanh MLP (1377 FP32 parameters:
- * W1[32][8], b1[32], W2[32][32], b2[32], w3[32], b3; weights run in BF16) on the normalised
- * features (raw_k - shift[k]) * scale[k] of raw = [Pi_xx, Pi_yy, Pi_zz, Pi_xy, Pi_xz, Pi_yz,
- * rho - 1, |Pi|] (Pi = non-equilibrium stress); nu_t = out_scale * y and
- * tau = max(3 (nu + nu_t) + 1/2, tau_min), tau_min > 1/2.  A non-finite output falls back to
- * Smagorinsky (cs from params.lbm; plain BGK when cs = 0), which inlet/outlet nodes use too.
+/* Learned eddy-viscosity closure for fluid nodes: an 8-32-32-1 MLP (1377 FP32 parameters:
+ * W1[32][8], b1[32], W2[32][32], b2[32], w3[32], b3; weights BF16, biases FP32, FP32
+ * accumulation, activation tanh of the BF16-rounded pre-activation, in BF16; evaluated on the
+ * tensor cores inside the collide kernel) on the normalised features
+ * (raw_k - shift[k]) * scale[k] of raw = [Pi_xx, Pi_yy, Pi_zz, Pi_xy, Pi_xz, Pi_yz, rho - 1,
+ * |Pi|] (Pi = non-equilibrium stress).  nu_t = max(out_scale * y, nu_smag), nu_smag the
+ * reference's Smagorinsky eddy viscosity with params.lbm's cs (no floor when cs = 0), and
+ * tau = max(3 (nu + nu_t) + 1/2, tau_min), tau_min > 1/2.  A non-finite output leaves the
+ * Smagorinsky rate (plain BGK when cs = 0), which inlet/outlet nodes use too.
  * params = NULL removes the closure. */
 tlbm_status tlbm_set_closure_mlp(tlbm_handle* h, const float* params, const float* scale,
                                  const float* shift, float out_scale, float tau_min);

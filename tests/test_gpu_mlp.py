@@ -136,6 +136,10 @@ def test_closure_pipeline_small():
     assert out["fine_finite"]
     assert out["loss_final"] < out["loss_initial"]
     assert out["learned"]["finite"] and out["smagorinsky"]["finite"]
+    # what the trained network gains over the method without it (plain BGK): a finite run, and
+    # a smaller error where plain BGK survives
+    err = lambda e: e["profile_err"] + e["spectrum_log_err"]
+    assert (not out["none"]["finite"]) or err(out["learned"]) <= err(out["none"])
 
 
 def test_fused_tensor_core_closure_matches_oracle():

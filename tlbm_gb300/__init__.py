@@ -44,7 +44,7 @@ class Options(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_int), ("precision", ctypes.c_int),
                 ("arithmetic", ctypes.c_int), ("closure", ctypes.c_int),
                 ("block_x", ctypes.c_int), ("block_y", ctypes.c_int), ("device", ctypes.c_int),
-                ("reserved", ctypes.c_int * 9)]
+                ("rbgk", ctypes.c_int), ("reserved", ctypes.c_int * 8)]
 
 
 class Problem(ctypes.Structure):
@@ -149,7 +149,8 @@ def declared_symbols(header: str = HEADER) -> list[str]:
     return sorted(set(re.findall(r"\b(tlbm_[a-z_0-9]+)\s*\(", text)))
 
 
-def options(precision="f32", arithmetic=None, block_x=0, block_y=0, device=0) -> Options:
+def options(precision="f32", arithmetic=None, block_x=0, block_y=0, device=0,
+            rbgk=False) -> Options:
     o = Options()
     library().tlbm_default_options(ctypes.byref(o))
     o.precision = PREC[precision]
@@ -157,6 +158,7 @@ def options(precision="f32", arithmetic=None, block_x=0, block_y=0, device=0) ->
         arithmetic = "fast" if precision in ("bf16", "f16") else "reference"
     o.arithmetic = ARITH[arithmetic]
     o.block_x, o.block_y, o.device = block_x, block_y, device
+    o.rbgk = int(bool(rbgk))
     return o
 
 
@@ -172,7 +174,8 @@ class TLBMPartition:
 
     def __init__(self, workdir: str = ".", rank: int = 0, size: int = 1 << 20,
                  precision: str | None = None, arithmetic: str | None = None,
-                 block_x: int = 0, block_y: int = 0, device: int = 0, _handle=None):
+                 block_x: int = 0, block_y: int = 0, device: int = 0, rbgk: bool = False,
+                 _handle=None):
         self._L = library()
         self._h = ctypes.c_void_p()
         self.workdir = workdir
@@ -182,7 +185,7 @@ class TLBMPartition:
             # like the reference binary: defaults, optionally overridden by workdir/tlbm.cfg
             _check(self._L.tlbm_create(workdir.encode(), rank, size, ctypes.byref(self._h)))
         else:
-            o = options(precision or "f32", arithmetic, block_x, block_y, device)
+            o = options(precision or "f32", arithmetic, block_x, block_y, device, rbgk)
             _check(self._L.tlbm_create_ex(workdir.encode(), rank, size, ctypes.byref(o),
                                           ctypes.byref(self._h)))
         try:
@@ -194,11 +197,12 @@ class TLBMPartition:
 
     @classmethod
     def from_arrays(cls, problem: Problem, nd_type, parts=None, workdir=None,
-                    precision="f64", arithmetic=None, block_x=0, block_y=0, device=0):
+                    precision="f64", arithmetic=None, block_x=0, block_y=0, device=0,
+                    rbgk=False):
         L = library()
         nd = np.ascontiguousarray(nd_type, dtype=np.int32)
         pp = None if parts is None else np.ascontiguousarray(parts, dtype=np.int32)
-        o = options(precision, arithmetic, block_x, block_y, device)
+        o = options(precision, arithmetic, block_x, block_y, device, rbgk)
         h = ctypes.c_void_p()
         _check(L.tlbm_create_from_arrays(ctypes.byref(problem), nd.ctypes.data,
                                          None if pp is None else pp.ctypes.data,

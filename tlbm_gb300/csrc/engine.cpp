@@ -168,6 +168,8 @@ Status apply_config_file(const std::string& path, tlbm_options* opt) {
       opt->block_y = std::atoi(val.c_str());
     } else if (key == "device") {
       opt->device = std::atoi(val.c_str());
+    } else if (key == "rbgk") {
+      opt->rbgk = std::atoi(val.c_str()) != 0;
     } else {
       return Status::err(TLBM_ERR_INVALID_ARGUMENT, path + ": unknown key " + key);
     }
@@ -291,6 +293,10 @@ Status Engine::init(const int32_t* nd_type, const int32_t* parts, int size) {
   if (ref_arith_ && (store_ == kStoreBF16 || store_ == kStoreF16))
     return Status::err(TLBM_ERR_INVALID_ARGUMENT,
                        "16-bit storage has no reference arithmetic; use TLBM_ARITH_FAST");
+  if (opt_.rbgk && ref_arith_)
+    return Status::err(TLBM_ERR_UNSUPPORTED,
+                       "the regularised BGK collision has no reference arithmetic (the reference "
+                       "streams without relaxation for dynamics 2): use TLBM_ARITH_FAST");
   if (opt_.closure != TLBM_CLOSURE_PARAMS)
     return Status::err(TLBM_ERR_UNSUPPORTED, "closure option not available");
   sb_ = store_bytes(store_);
@@ -418,6 +424,7 @@ Status Engine::init(const int32_t* nd_type, const int32_t* parts, int size) {
   pb_.u_bc = prob_.u_lbm;
   pb_.rho_bc = prob_.rho_lbm;
   pb_.dynamics = prob_.dynamics;
+  pb_.rbgk = (opt_.rbgk && prob_.dynamics == 2) ? 1 : 0;
   pb_.has_type5 = has_type5_ ? 1 : 0;
   fill_derived(pb_, q_, sb_);
 

@@ -24,6 +24,7 @@ struct DevProblem {
   // thread would spend FP64-pipe slots on it)
   float omega_f, cs_f, u_bc_f, rho_bc_f, nu_f;
   int dynamics;
+  int rbgk;  // dynamics 2 runs the regularised BGK collision (fast arithmetic)
   int has_type5;
   // byte offset, from a cell's own population of speed 0, of the population of speed i that an
   // interior cell (no face of the box) pulls: i*n*bytes - (ex + ey*nx + ez*nx*ny)*bytes
@@ -32,6 +33,9 @@ struct DevProblem {
   const double* inlet_d;
   const float* inlet_f;
 };
+
+// whether nodes relax: LBGK, or the regularised BGK of dynamics 2
+TLBM_HD bool relaxes(const DevProblem& p) { return p.dynamics == 1 || p.rbgk; }
 
 // problem parameters in the compute type
 template <class C>

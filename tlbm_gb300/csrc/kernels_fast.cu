@@ -55,6 +55,7 @@ __global__ void __launch_bounds__(128, kMlpMinBlocks<K>)
   bool fluid = false;
   C f[L::Q];
   C rho = 0, ux = 0, uy = 0, uz = 0, q2 = 0;
+  C pi[6];  // kept across the network only for the regularised collision
   float xin[mlp::kIn] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   if (in) {
     typename S::T raw[L::Q];
@@ -70,7 +71,9 @@ __global__ void __launch_bounds__(128, kMlpMinBlocks<K>)
       uy = st.uy;
       uz = st.uz;
       q2 = st.q2;
-      if (pb.dynamics == 1) fast::closure_inputs<L, C>(st, cl, xin);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) pi[k] = st.pi[k];
+      if (relaxes(pb)) fast::closure_inputs<L, C>(st, cl, xin);
     } else {
       if (pb.cs > 0)
         boundary_node<L, K, true>(a, x, y, c, t, raw, rho, ux, uy, uz);
@@ -82,10 +85,10 @@ __global__ void __launch_bounds__(128, kMlpMinBlocks<K>)
   __syncthreads();  // the network is in shared memory
   const int warp = tid >> 5, lane = tid & 31;
   float net = 0.f;
-  if (__any_sync(0xFFFFFFFFu, fluid && pb.dynamics == 1))
+  if (__any_sync(0xFFFFFFFFu, fluid && relaxes(pb)))
     net = mlp::forward_warp(sw, xs[warp], ys[warp], xin, lane);
   if (!fluid) return;
-  if (pb.dynamics == 1) {
+  if (relaxes(pb)) {
     launder(ux);
     launder(uy);
     launder(uz);
@@ -97,7 +100,13 @@ __global__ void __launch_bounds__(128, kMlpMinBlocks<K>)
     fast::fluid_pair_terms<L, C>(st);
     const C omega = fast::closure_omega<C>(net, cl, Par<C>::omega(pb), Par<C>::cs(pb),
                                            Par<C>::nu(pb), q2);
-    fast::fluid_relax<L, C>(f, st, omega);
+    if (pb.rbgk) {
+#pragma unroll
+      for (int k = 0; k < 6; ++k) st.pi[k] = pi[k];
+      fast::fluid_relax_reg<L, C>(f, st, omega);
+    } else {
+      fast::fluid_relax<L, C>(f, st, omega);
+    }
   }
   store_cell<L, K>(a, c, f);
   if (a.time_avg) accumulate_avg<C>(a, c, rho, ux, uy, uz);

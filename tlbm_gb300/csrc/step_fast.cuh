@@ -4,7 +4,8 @@
 // (kernels_ensemble.cu), so both compute every cell with the same instructions.  The cell
 // pulls its Q populations from c - e_i (periodic), branches on its node type, collides in
 // registers and stores at c:
-//   fluid        -> pair-form BGK / Smagorinsky (physics_fast.cuh: fluid_collide)
+//   fluid        -> pair-form BGK / Smagorinsky, optionally regularised (physics_fast.cuh:
+//                   fluid_collide)
 //   solid        -> bounce-back of the raw stored values, no collision
 //   inlet/outlet -> the reference's density/velocity rule, non-equilibrium bounce-back of the
 //                   unknown speeds, then BGK / Smagorinsky
@@ -140,10 +141,13 @@ __device__ __forceinline__ void boundary_node(const StepArgs& a, int x, int y, i
   fast::equilibrium<L, C>(rho, ux, uy, uz, feq);
   if (t == kInlet) fast::nebb<L, C, true>(f, feq);
   if (t == kOutlet) fast::nebb<L, C, false>(f, feq);
-  if (pb.dynamics == 1) {
+  if (relaxes(pb)) {
     C om = Par<C>::omega(pb);
     if (kSmag) om = fast::smagorinsky_omega<L, C>(f, feq, Par<C>::cs(pb), Par<C>::nu(pb));
-    fast::relax<L, C>(f, feq, om);
+    if (pb.rbgk)
+      fast::relax_reg<L, C>(f, feq, om);
+    else
+      fast::relax<L, C>(f, feq, om);
   }
   store_cell<L, K>(a, c, f);
 }
@@ -174,7 +178,7 @@ __device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z
     C f[L::Q];
     unpack<L, K>(raw, f);
     fast::fluid_collide<L, C, kClosure>(f, Par<C>::omega(pb), Par<C>::cs(pb), Par<C>::nu(pb),
-                                        pb.dynamics == 1, rho, ux, uy, uz);
+                                        relaxes(pb), pb.rbgk != 0, rho, ux, uy, uz);
     store_cell<L, K>(a, c, f);
   } else if (kClosure == fast::kClosureSmag) {
     boundary_node<L, K, true>(a, x, y, c, t, raw, rho, ux, uy, uz);
