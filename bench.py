@@ -370,6 +370,30 @@ def ensemble_line(device, steps=200, seed=7):
             "launches_per_step": launches / steps, "all_finite": finite}
 
 
+def closure_line(g, p, device, steps=50, seed=3):
+    """Cost per step of the learned closure (tensor-core MLP fused in collide, Smagorinsky floor)
+    against plain Smagorinsky on the same geometry, FP32 storage."""
+    import tlbm_gb300 as T
+    from tlbm_gb300 import geometry as G
+    from tlbm_gb300 import mlp_params
+
+    pv = G.params_lattice_units(g, "D3Q19", p.u_lbm, 200.0, g.lo, steps, cs=p.cs, rho_lbm=1.0)
+    nu = (1.0 / pv.omega - 0.5) / 3.0
+    res = {}
+    for name in ("smagorinsky", "learned"):
+        part = T.TLBMPartition.from_arrays(T.problem_from_params(pv), g.nd_type, precision="f32",
+                                           arithmetic="fast", device=device)
+        if name == "learned":
+            part.set_closure_mlp(mlp_params.xavier(seed), np.ones(8), np.zeros(8), 1e-4,
+                                 3.0 * nu + 0.5 + 1e-6)
+        part.run(0, 4)
+        res[name] = part.time_steps(4, steps) / steps
+        part.close()
+    return {"precision": "f32", "ms_per_step": {k: round(v, 4) for k, v in res.items()},
+            "learned_over_smagorinsky": round(res["learned"] / res["smagorinsky"], 3),
+            "learned_mlups": round(g.num_nodes / (res["learned"] / 1e3) / 1e6, 1)}
+
+
 def extras(args, g, p, dist):
     from tlbm_gb300 import geometry as G
     from tlbm_gb300 import studies
@@ -380,6 +404,7 @@ def extras(args, g, p, dist):
         out["lines"].append(variant_line(g, p, lat, prec, "fast", 50, dist.local))
     out["lines"].append(variant_line(g, p, "D3Q19", "f64", "reference", 20, dist.local))
     out["ensemble"] = ensemble_line(dist.local)
+    out["closure"] = closure_line(g, p, dist.local)
     # storage-precision error after 1000 steps on a 256x128x128 pack, against the FP64
     # reference-exact run (byte-identical to the CPU reference)
     gs = G.random_sphere_pack(256, 128, 128, 4.0, 12.0, 0.7, seed=args.seed)
