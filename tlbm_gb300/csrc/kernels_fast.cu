@@ -10,13 +10,13 @@
 namespace tlbm {
 namespace {
 
-template <class L, int K, int kClosure>
+template <class L, int K, int kClosure, bool kReg>
 __global__ void __launch_bounds__(128) k_step_fast(StepArgs a) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
   if (x >= a.pb.nx || y >= a.pb.ny) return;
-  cell_step<L, K, kClosure>(a, x, y, z);
+  cell_step<L, K, kClosure, kReg>(a, x, y, z);
 }
 
 // an opaque copy: the compiler cannot reuse values computed from v before this point
@@ -75,10 +75,14 @@ __global__ void __launch_bounds__(128, kMlpMinBlocks<K>)
       for (int k = 0; k < 6; ++k) pi[k] = st.pi[k];
       if (relaxes(pb)) fast::closure_inputs<L, C>(st, cl, xin);
     } else {
-      if (pb.cs > 0)
-        boundary_node<L, K, true>(a, x, y, c, t, raw, rho, ux, uy, uz);
+      if (pb.cs > 0 && pb.rbgk)
+        boundary_node<L, K, true, true>(a, x, y, c, t, raw, rho, ux, uy, uz);
+      else if (pb.cs > 0)
+        boundary_node<L, K, true, false>(a, x, y, c, t, raw, rho, ux, uy, uz);
+      else if (pb.rbgk)
+        boundary_node<L, K, false, true>(a, x, y, c, t, raw, rho, ux, uy, uz);
       else
-        boundary_node<L, K, false>(a, x, y, c, t, raw, rho, ux, uy, uz);
+        boundary_node<L, K, false, false>(a, x, y, c, t, raw, rho, ux, uy, uz);
       if (a.time_avg) accumulate_avg<C>(a, c, rho, ux, uy, uz);
     }
   }
@@ -205,10 +209,14 @@ cudaError_t step_lk(const StepArgs& a, const Launch& l) {
   const dim3 g = grid_of(a.pb, l), b(l.bx, l.by, 1);
   if (a.closure)
     k_step_fast_mlp<L, K><<<g, b, 0, l.stream>>>(a, *static_cast<const mlp::Closure*>(a.closure));
+  else if (a.pb.cs > 0 && a.pb.rbgk)
+    k_step_fast<L, K, fast::kClosureSmag, true><<<g, b, 0, l.stream>>>(a);
   else if (a.pb.cs > 0)
-    k_step_fast<L, K, fast::kClosureSmag><<<g, b, 0, l.stream>>>(a);
+    k_step_fast<L, K, fast::kClosureSmag, false><<<g, b, 0, l.stream>>>(a);
+  else if (a.pb.rbgk)
+    k_step_fast<L, K, fast::kClosureNone, true><<<g, b, 0, l.stream>>>(a);
   else
-    k_step_fast<L, K, fast::kClosureNone><<<g, b, 0, l.stream>>>(a);
+    k_step_fast<L, K, fast::kClosureNone, false><<<g, b, 0, l.stream>>>(a);
   return cudaGetLastError();
 }
 

@@ -85,8 +85,9 @@ __device__ __forceinline__ void store_cell(const StepArgs& a, int c,
 }
 
 // every node type but fluid: solid bounce-back, inlet/outlet reconstruction and relaxation,
-// the moving-wall nudge.  kSmag: boundary nodes relax at the Smagorinsky rate.
-template <class L, int K, bool kSmag>
+// the moving-wall nudge.  kSmag: boundary nodes relax at the Smagorinsky rate; kReg: with the
+// regularised collision.
+template <class L, int K, bool kSmag, bool kReg>
 __device__ __forceinline__ void boundary_node(const StepArgs& a, int x, int y, int c, uint8_t t,
                                               const typename Store<K>::T (&raw)[L::Q],
                                               typename Store<K>::C& rho,
@@ -144,7 +145,7 @@ __device__ __forceinline__ void boundary_node(const StepArgs& a, int x, int y, i
   if (relaxes(pb)) {
     C om = Par<C>::omega(pb);
     if (kSmag) om = fast::smagorinsky_omega<L, C>(f, feq, Par<C>::cs(pb), Par<C>::nu(pb));
-    if (pb.rbgk)
+    if constexpr (kReg)
       fast::relax_reg<L, C>(f, feq, om);
     else
       fast::relax<L, C>(f, feq, om);
@@ -163,8 +164,8 @@ __device__ __forceinline__ void accumulate_avg(const StepArgs& a, int c, C rho, 
 }
 
 // kClosure: fast::kClosureNone (BGK) or kClosureSmag (the learned closure has its own kernel,
-// kernels_fast.cu: k_step_fast_mlp)
-template <class L, int K, int kClosure>
+// kernels_fast.cu: k_step_fast_mlp); kReg: regularised collision (dynamics 2 with the option)
+template <class L, int K, int kClosure, bool kReg = false>
 __device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z) {
   using S = Store<K>;
   using C = typename S::C;
@@ -177,13 +178,12 @@ __device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z
   if (t == kFluid) {
     C f[L::Q];
     unpack<L, K>(raw, f);
-    fast::fluid_collide<L, C, kClosure>(f, Par<C>::omega(pb), Par<C>::cs(pb), Par<C>::nu(pb),
-                                        relaxes(pb), pb.rbgk != 0, rho, ux, uy, uz);
+    fast::fluid_collide<L, C, kClosure, kReg>(f, Par<C>::omega(pb), Par<C>::cs(pb),
+                                              Par<C>::nu(pb), relaxes(pb), rho, ux, uy, uz);
     store_cell<L, K>(a, c, f);
-  } else if (kClosure == fast::kClosureSmag) {
-    boundary_node<L, K, true>(a, x, y, c, t, raw, rho, ux, uy, uz);
   } else {
-    boundary_node<L, K, false>(a, x, y, c, t, raw, rho, ux, uy, uz);
+    boundary_node<L, K, kClosure == fast::kClosureSmag, kReg>(a, x, y, c, t, raw, rho, ux, uy,
+                                                              uz);
   }
   if (a.time_avg) accumulate_avg<C>(a, c, rho, ux, uy, uz);
 }
