@@ -504,11 +504,14 @@ def channel_sphere_32x32x128_params(num_ts=2000, plot_freq=2000, lattice="D3Q19"
     return p
 
 
-def ensemble_channels(n: int = 64, seed: int = 7, u_in: float = 0.04, num_ts: int = 2000):
+def ensemble_channels(n: int = 64, seed: int = 7, u_in: float = 0.04, num_ts: int = 2000,
+                      cs: float = 0.1):
     """The batched-ensemble workload: ``n`` independent channels, each with Nx = Ny drawn from
     {32, 48, 64}, Nz uniform in [64, 256], lattice D3Q15 or D3Q19, Re uniform in [50, 500] on
     the sphere diameter, one sphere of radius Nx/6 on the channel axis at a seeded height in
-    [Nz/4, Nz/2], solid x/y walls, z==0 inlet (u_in) and z==Nz-1 outlet (rho = 1).
+    [Nz/4, Nz/2], solid x/y walls, z==0 inlet (u_in) and z==Nz-1 outlet (rho = 1).  The
+    channels relax with the Smagorinsky model (cs): at these Reynolds numbers tau is 0.503 to
+    0.55, and plain BGK from rest diverges in 60 of the 64 channels within 2000 steps.
     Returns a list of (Geometry, Params)."""
     rng = np.random.default_rng(seed)
     out = []
@@ -520,6 +523,6 @@ def ensemble_channels(n: int = 64, seed: int = 7, u_in: float = 0.04, num_ts: in
         r = nx / 6.0
         zc = float(rng.uniform(nz / 4.0, nz / 2.0))
         g = sphere_in_box(nx, nx, nz, r, (nx - 1) / 2.0, (nx - 1) / 2.0, zc, walls=True)
-        p = params_lattice_units(g, lattice, u_in, re, 2.0 * r, num_ts)
+        p = params_lattice_units(g, lattice, u_in, re, 2.0 * r, num_ts, cs=cs)
         out.append((g, p))
     return out
