@@ -1,0 +1,48 @@
+"""The reference's own acceptance check, python/validate.py (relative 1-norm of |u| against a
+gold standard made by python/gen_gold_standard.py), applied to the GPU engine's dump files:
+the gold standard is the reference's FP32 dump of a golden case."""
+
+import numpy as np
+import pytest
+
+import tlbm_gb300 as T
+from cases_util import CASES, write_case_inputs
+from conftest import golden_arrays
+from tlbm_gb300 import build as B
+from tlbm_gb300 import io as TIO
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    B.build()
+    T.library()
+
+
+def reference_gold(name):
+    """gen_gold_standard.py on the reference's last FP32 dump (arrays stored by the fixture)."""
+    z = golden_arrays(name)
+    order = z["ordering"]
+    u = []
+    for k in ("ux", "uy", "uz"):
+        a = np.zeros_like(z["f32_" + k])
+        a[order] = z["f32_" + k]
+        u.append(a)
+    return np.sqrt(u[0] ** 2 + u[1] ** 2 + u[2] ** 2)
+
+
+@pytest.mark.parametrize("name", ["q19_sphere_bgk", "q27_sphere_smag"])
+@pytest.mark.parametrize("form,tol", [(("f32", "reference"), 0.0), (("f32", "fast"), 1e-4),
+                                      (("f16", "fast"), 5e-3), (("bf16", "fast"), 2e-2)])
+def test_validate_py_against_reference_gold(name, form, tol, tmp_path):
+    gold = reference_gold(name)
+    write_case_inputs(name, str(tmp_path))
+    part = T.TLBMPartition(str(tmp_path), precision=form[0], arithmetic=form[1])
+    T.run_like_tlbmexec(part)
+    part.close()
+    last = CASES[name]["summary"]["f32"]["last_dump"]
+    # the 16-bit forms dump float32 files, like FP32 runs
+    r = TIO.validate(str(tmp_path), last, gold)
+    print("%s %s/%s: validate.py relative 1-norm difference = %.3g" % (name, *form, r["rel"]))
+    assert r["rel"] <= tol

@@ -1,4 +1,5 @@
-"""Output-file helpers: read dumps in global order and write restart data.
+"""Output-file helpers: read dumps in global order, write restart data, and the gold-standard
+check of python/gen_gold_standard.py and python/validate.py.
 
 The solver writes each field in partition-major order with ``ordering.b_dat`` giving the global
 node number of every position (src/TLBM_Partition.cpp:542-561, :608-683).  The reference's
@@ -35,3 +36,21 @@ def create_restart(workdir: str, dump: int, out_dir: str | None = None, dtype=np
     for src, dst in (("ux", "ux"), ("uy", "uy"), ("uz", "uz"), ("density", "rho")):
         d[src].astype(np.float32).tofile(os.path.join(out_dir, "restart_%s.b_dat" % dst))
     return out_dir
+
+
+def gold_standard(workdir: str, dump: int, dtype=np.float32) -> np.ndarray:
+    """|u| of dump `dump` in global order, as python/gen_gold_standard.py:13-34 computes it
+    (float32 squares and sum, float32 sqrt)."""
+    d = read_dump(workdir, dump, dtype, fields=("ux", "uy", "uz"))
+    return np.sqrt(d["ux"] ** 2 + d["uy"] ** 2 + d["uz"] ** 2)
+
+
+def validate(workdir: str, dump: int, gold: np.ndarray, dtype=np.float32) -> dict:
+    """python/validate.py:14-44: relative and absolute 1-norm differences of |u| of dump
+    `dump` against a gold-standard array."""
+    umag = gold_standard(workdir, dump, dtype)
+    gold = np.asarray(gold)
+    dif_abs = float(np.linalg.norm(umag - gold, ord=1))
+    norm = float(np.linalg.norm(gold, ord=1))
+    return {"l1_test": float(np.linalg.norm(umag, ord=1)), "l1_gold": norm,
+            "rel": dif_abs / norm, "abs": dif_abs}
