@@ -45,7 +45,7 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=30)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--lattice", default="D3Q19")
-    ap.add_argument("--precision", default="f64", choices=["f64", "f32", "bf16", "f16"])
+    ap.add_argument("--precision", default="f64", choices=["f64", "f32", "bf16", "f16", "bf16m"])
     ap.add_argument("--arithmetic", default="fast", choices=["fast", "reference"])
     ap.add_argument("--nx", type=int, default=512)
     ap.add_argument("--ny", type=int, default=256)
@@ -203,6 +203,13 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def cell_bytes(q, precision):
+    """Algorithmic bytes of one cell update: read and write Q populations, read the node type;
+    the moment-shifted BF16 form also reads and writes a float4 per cell."""
+    sb = {"f64": 8, "f32": 4, "bf16": 2, "f16": 2, "bf16m": 2}[precision]
+    return 2 * q * sb + 1 + (32 if precision == "bf16m" else 0)
+
+
 def traffic_per_cell(lattice, precision):
     """DRAM bytes per cell-update of the step kernel from the committed ncu summary, if any."""
     path = os.path.join(HERE, "profiles", "traffic.json")
@@ -270,8 +277,7 @@ def run_ours(args, dist):
     mass = part.mass()
     part.close()
 
-    sb = {"f64": 8, "f32": 4, "bf16": 2, "f16": 2}[args.precision]
-    bytes_per_cell = 2 * q * sb + 1
+    bytes_per_cell = cell_bytes(q, args.precision)
     step_s = ms_max / 1e3 / args.steps
     value = n * args.steps * dist.world / (ms_max / 1e3) / 1e6
     peak, peak_kind = peaks()
@@ -288,7 +294,8 @@ def run_ours(args, dist):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": {"f64": "f64", "f32": "f32", "bf16": "bf16-storage/f32", "f16":
+        "dtype": {"f64": "f64", "f32": "f32", "bf16": "bf16-storage/f32", "bf16m":
+                  "bf16-moment-shifted-storage/f32", "f16":
                   "f16-storage/f32"}[args.precision],
         "data": "synthetic",
         "config": {
@@ -338,12 +345,12 @@ def variant_line(g, p, lattice, precision, arithmetic, steps, device):
     ms = part.time_steps(4, steps)
     part.close()
     q = int(lattice[3:])
-    sb = {"f64": 8, "f32": 4, "bf16": 2, "f16": 2}[precision]
+    bpc = cell_bytes(q, precision)
     mlups = g.num_nodes * steps / (ms / 1e3) / 1e6
     peak, _ = peaks()
     return {"lattice": lattice, "precision": precision, "arithmetic": arithmetic,
             "mlups": round(mlups, 1),
-            "hbm_frac": round(mlups * 1e6 * (2 * q * sb + 1) / 1e9 / peak, 4)}
+            "hbm_frac": round(mlups * 1e6 * bpc / 1e9 / peak, 4)}
 
 
 def ensemble_line(device, steps=200, seed=7):
@@ -400,7 +407,7 @@ def extras(args, g, p, dist):
 
     out = {"lines": []}
     for lat, prec in (("D3Q27", "f64"), ("D3Q19", "f32"), ("D3Q27", "f32"), ("D3Q19", "bf16"),
-                      ("D3Q19", "f16")):
+                      ("D3Q19", "f16"), ("D3Q19", "bf16m")):
         out["lines"].append(variant_line(g, p, lat, prec, "fast", 50, dist.local))
     out["lines"].append(variant_line(g, p, "D3Q19", "f64", "reference", 20, dist.local))
     out["ensemble"] = ensemble_line(dist.local)
@@ -409,7 +416,7 @@ def extras(args, g, p, dist):
     # reference-exact run (byte-identical to the CPU reference)
     gs = G.random_sphere_pack(256, 128, 128, 4.0, 12.0, 0.7, seed=args.seed)
     ps = G.params_lattice_units(gs, "D3Q19", 0.04, 200.0, gs.lo, 1000, cs=0.1, rho_lbm=1.0)
-    res = studies.precision_study(gs, ps, 1000, forms=("f64-fast", "f32", "f16", "bf16"),
+    res = studies.precision_study(gs, ps, 1000, forms=("f64-fast", "f32", "f16", "bf16", "bf16m"),
                                   device=dist.local)
     out["precision_1000_steps_256x128x128"] = {
         k: {kk: (round(vv, 9) if isinstance(vv, float) else vv) for kk, vv in v.items()}

@@ -48,7 +48,10 @@ typedef enum {
   TLBM_PREC_F64 = 0,  /* double populations, double arithmetic */
   TLBM_PREC_F32 = 1,  /* float populations, float arithmetic (the reference default) */
   TLBM_PREC_BF16 = 2, /* bfloat16 storage of f_i - w_i, float collision */
-  TLBM_PREC_F16 = 3   /* half storage of f_i - w_i, float collision */
+  TLBM_PREC_F16 = 3,  /* half storage of f_i - w_i, float collision */
+  TLBM_PREC_BF16M = 4 /* bfloat16 storage of f_i - w_i (rho + e_i.(3 j)) with (rho, 3 j) of the
+                         storing cell kept as FP32 beside the populations (16 B per cell), float
+                         collision */
 } tlbm_precision;
 
 /* Arithmetic flavour for TLBM_PREC_F64 / TLBM_PREC_F32. */

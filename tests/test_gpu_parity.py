@@ -105,9 +105,11 @@ def test_fast_fp64_small_within_1e12(name, steps, tmp_path):
         assert rel_inf(a, b) <= 1e-12, fn
 
 
-@pytest.mark.parametrize("prec,tol", [("f32", 1e-4), ("f16", 2e-2), ("bf16", 1e-1)])
+@pytest.mark.parametrize("prec,tol", [("f32", 1e-4), ("f16", 2e-2), ("bf16", 1e-1),
+                                      ("bf16m", 1e-3)])
 def test_reduced_precision_velocity_error(prec, tol, tmp_path):
-    """Velocity-magnitude relative L2 error against FP64 after 2000 steps of the channel."""
+    """Velocity-magnitude relative L2 error against FP64 after 2000 steps of the channel; the
+    moment-shifted BF16 storage keeps it within 1e-3."""
     ref, fast = fast_vs_reference("channel32_q19_2000", prec, tmp_path)
     umag = lambda m: np.sqrt(m[0].astype(np.float64) ** 2 + m[1] ** 2 + m[2] ** 2)
     err = rel_l2(umag(fast), umag(ref))
@@ -205,7 +207,7 @@ def test_graph_run_equals_single_steps():
     assert b.kernel_launches() >= 13
 
 
-@pytest.mark.parametrize("prec", ["f64", "f32", "bf16", "f16"])
+@pytest.mark.parametrize("prec", ["f64", "f32", "bf16", "f16", "bf16m"])
 def test_mass_reduction(prec):
     """FP64 mass of all populations: equals a host sum of the exported populations, is
     deterministic, and is conserved on a closed periodic box without boundaries.  D3Q27: its
@@ -218,8 +220,8 @@ def test_mass_reduction(prec):
     m1 = part.mass()
     assert m1 == part.mass()
     host = part.populations(1).astype(np.float64).sum()
-    assert abs(m1 - host) <= 1e-12 * abs(host) + (1e-3 if prec in ("bf16", "f16") else 0)
-    tol = {"f64": 1e-13, "f32": 1e-5, "bf16": 1e-2, "f16": 1e-3}[prec]
+    assert abs(m1 - host) <= 1e-12 * abs(host) + (1e-3 if prec in ("bf16", "f16", "bf16m") else 0)
+    tol = {"f64": 1e-13, "f32": 1e-5, "bf16": 1e-2, "f16": 1e-3, "bf16m": 1e-3}[prec]
     assert abs(m1 - m0) <= tol * m0
 
 
@@ -278,3 +280,30 @@ def test_restart_from_dump_files(tmp_path):
     assert r.returncode == 0, r.stderr
     oracle_lib.run_dir(d2, "f32")
     assert output_digests(d1) == output_digests(d2)
+
+
+@pytest.mark.parametrize("q", [15, 19, 27])
+def test_bf16m_restart_and_steps_close_to_f32(q):
+    """Moment-shifted BF16 storage: a restart from random fields (each slot's shift comes from
+    its own node's fields) and 5 steps stay within the remainders' rounding of the FP32 run,
+    on a box with every node type; plain BGK, Smagorinsky and the closure-free boundary paths
+    read and write through the float4 of moments."""
+    geom, p = small_problem(q, nx=24, ny=10, nz=12, seed=q, cs=0.1)
+    n = geom.num_nodes
+    rng = np.random.default_rng(q)
+    f = [rng.uniform(-0.03, 0.03, n), rng.uniform(-0.03, 0.03, n), rng.uniform(0.0, 0.06, n),
+         rng.uniform(0.98, 1.02, n)]
+    out = {}
+    for prec in ("f32", "bf16m", "bf16"):
+        part = T.TLBMPartition.from_arrays(T.problem_from_params(p), geom.nd_type,
+                                           precision=prec, arithmetic="fast")
+        part.load_restart(*f)
+        part.run(0, 5)
+        out[prec] = (part.populations(0).astype(np.float64), part.macros(), part.force())
+        part.close()
+    err_m = np.abs(out["bf16m"][0] - out["f32"][0]).max()
+    err_b = np.abs(out["bf16"][0] - out["f32"][0]).max()
+    print("D3Q%d populations vs FP32: bf16m %.2e, bf16 %.2e" % (q, err_m, err_b))
+    assert err_m <= 2e-5 and err_m < err_b / 4
+    for a, b in zip(out["bf16m"][1], out["f32"][1]):
+        assert np.abs(np.asarray(a, np.float64) - b).max() <= 1e-4

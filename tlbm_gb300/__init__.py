@@ -29,7 +29,7 @@ HEADER = os.path.join(os.path.dirname(HERE), "include", "tlbm.h")
 # status codes (include/tlbm.h)
 OK, ERR_IO, ERR_INVALID_ARGUMENT, ERR_FORMAT, ERR_OUT_OF_RANGE, ERR_CUDA, ERR_NUMERIC, \
     ERR_UNSUPPORTED, ERR_TIMEOUT, ERR_NO_MEMORY = range(10)
-PREC = {"f64": 0, "f32": 1, "bf16": 2, "f16": 3}
+PREC = {"f64": 0, "f32": 1, "bf16": 2, "f16": 3, "bf16m": 4}
 ARITH = {"reference": 0, "fast": 1}
 
 
@@ -155,7 +155,7 @@ def options(precision="f32", arithmetic=None, block_x=0, block_y=0, device=0,
     library().tlbm_default_options(ctypes.byref(o))
     o.precision = PREC[precision]
     if arithmetic is None:
-        arithmetic = "fast" if precision in ("bf16", "f16") else "reference"
+        arithmetic = "fast" if precision in ("bf16", "f16", "bf16m") else "reference"
     o.arithmetic = ARITH[arithmetic]
     o.block_x, o.block_y, o.device = block_x, block_y, device
     o.rbgk = int(bool(rbgk))

@@ -157,6 +157,7 @@ Status apply_config_file(const std::string& path, tlbm_options* opt) {
       else if (val == "f32") opt->precision = TLBM_PREC_F32;
       else if (val == "bf16") opt->precision = TLBM_PREC_BF16;
       else if (val == "f16") opt->precision = TLBM_PREC_F16;
+      else if (val == "bf16m") opt->precision = TLBM_PREC_BF16M;
       else return Status::err(TLBM_ERR_INVALID_ARGUMENT, path + ": unknown precision " + val);
     } else if (key == "arithmetic") {
       if (val == "reference") opt->arithmetic = TLBM_ARITH_REFERENCE;
@@ -287,10 +288,11 @@ Status Engine::init(const int32_t* nd_type, const int32_t* parts, int size) {
     case TLBM_PREC_F32: store_ = kStoreF32; break;
     case TLBM_PREC_BF16: store_ = kStoreBF16; break;
     case TLBM_PREC_F16: store_ = kStoreF16; break;
+    case TLBM_PREC_BF16M: store_ = kStoreBF16M; break;
     default: return Status::err(TLBM_ERR_INVALID_ARGUMENT, "unknown precision option");
   }
   ref_arith_ = (opt_.arithmetic == TLBM_ARITH_REFERENCE);
-  if (ref_arith_ && (store_ == kStoreBF16 || store_ == kStoreF16))
+  if (ref_arith_ && (store_ == kStoreBF16 || store_ == kStoreF16 || store_ == kStoreBF16M))
     return Status::err(TLBM_ERR_INVALID_ARGUMENT,
                        "16-bit storage has no reference arithmetic; use TLBM_ARITH_FAST");
   if (opt_.rbgk && ref_arith_)
@@ -393,7 +395,7 @@ Status Engine::init(const int32_t* nd_type, const int32_t* parts, int size) {
   const size_t n = static_cast<size_t>(n_);
   TLBM_CUDA(cudaMalloc(&d_type_, n));
   TLBM_CUDA(cudaMemcpy(d_type_, types.data(), n, cudaMemcpyHostToDevice));
-  for (auto& p : d_f_) TLBM_CUDA(cudaMalloc(&p, n * q_ * sb_));
+  for (auto& p : d_f_) TLBM_CUDA(cudaMalloc(&p, buffer_bytes(store_, q_, n_)));
   for (auto& p : d_macro_) TLBM_CUDA(cudaMalloc(&p, n * ob_));
   for (auto& p : d_force_) TLBM_CUDA(cudaMalloc(&p, n * ob_));
   if (prob_.time_avg_flag == 1) {

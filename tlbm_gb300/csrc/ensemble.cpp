@@ -59,6 +59,8 @@ Status Ensemble::init(int n, const tlbm_problem* probs, const int32_t* const* nd
     case TLBM_PREC_F32: store_ = kStoreF32; break;
     case TLBM_PREC_BF16: store_ = kStoreBF16; break;
     case TLBM_PREC_F16: store_ = kStoreF16; break;
+    case TLBM_PREC_BF16M:
+      return Status::err(TLBM_ERR_UNSUPPORTED, "ensembles take f64, f32, bf16 or f16 storage");
     default: return Status::err(TLBM_ERR_INVALID_ARGUMENT, "unknown precision option");
   }
   sb_ = store_bytes(store_);

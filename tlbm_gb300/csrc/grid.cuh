@@ -29,6 +29,8 @@ struct DevProblem {
   // byte offset, from a cell's own population of speed 0, of the population of speed i that an
   // interior cell (no face of the box) pulls: i*n*bytes - (ex + ey*nx + ez*nx*ny)*bytes
   long long pull_off[27];
+  // the same offsets in cells, ex + ey*nx + ez*nx*ny (the pulled slot is c - pull_cell[i])
+  int pull_cell[27];
   // optional inlet velocity per (x, y) of the z = 0 plane (nx*ny values; null: uniform u_bc)
   const double* inlet_d;
   const float* inlet_f;
@@ -66,12 +68,16 @@ struct Par<float> {
 // fills the float copies and the interior pull offsets of `pb` for q speeds of `bytes` each
 template <class L>
 inline void fill_pull_offsets(DevProblem& pb, int bytes) {
-  for (int i = 0; i < 27; ++i) pb.pull_off[i] = 0;
-  for (int i = 0; i < L::Q; ++i)
-    pb.pull_off[i] = (static_cast<long long>(i) * pb.n -
-                      (L::ex(i) + static_cast<long long>(L::ey(i)) * pb.nx +
-                       static_cast<long long>(L::ez(i)) * pb.nxy)) *
-                     bytes;
+  for (int i = 0; i < 27; ++i) {
+    pb.pull_off[i] = 0;
+    pb.pull_cell[i] = 0;
+  }
+  for (int i = 0; i < L::Q; ++i) {
+    const long long d = L::ex(i) + static_cast<long long>(L::ey(i)) * pb.nx +
+                        static_cast<long long>(L::ez(i)) * pb.nxy;
+    pb.pull_off[i] = (static_cast<long long>(i) * pb.n - d) * bytes;
+    pb.pull_cell[i] = static_cast<int>(d);
+  }
 }
 
 inline void fill_derived(DevProblem& pb, int q, int bytes) {

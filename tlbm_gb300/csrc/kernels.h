@@ -10,8 +10,20 @@
 namespace tlbm {
 
 // storage kinds of the population arrays
-enum StoreKind : int { kStoreF64 = 0, kStoreF32 = 1, kStoreBF16 = 2, kStoreF16 = 3 };
+enum StoreKind : int {
+  kStoreF64 = 0,
+  kStoreF32 = 1,
+  kStoreBF16 = 2,
+  kStoreF16 = 3,
+  kStoreBF16M = 4,  // BF16 remainders after a per-cell moment shift (storage.cuh)
+};
 inline int store_bytes(int k) { return k == kStoreF64 ? 8 : (k == kStoreF32 ? 4 : 2); }
+// bytes of one population buffer: Q planes, then (moment-shifted kind) a float4 per cell
+inline size_t buffer_bytes(int k, int q, int64_t n) {
+  const size_t planes = static_cast<size_t>(n) * q * store_bytes(k);
+  if (k != kStoreBF16M) return planes;
+  return ((planes + 15) / 16) * 16 + static_cast<size_t>(n) * 16;
+}
 
 struct StepArgs {
   DevProblem pb;

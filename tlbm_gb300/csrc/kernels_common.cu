@@ -23,17 +23,25 @@ int blocks_for(int64_t n) {
 }
 
 template <class L, int K>
-__global__ void k_init_uniform(DevProblem pb, typename Store<K>::T* f, double rho) {
+__global__ void k_init_uniform(DevProblem pb, void* fv, double rho) {
   using S = Store<K>;
   using C = typename S::C;
   const size_t n = static_cast<size_t>(pb.n);
+  auto* f = static_cast<typename S::P*>(fv);
   TLBM_FOR_CELLS(c, pb.n) {
+    if constexpr (S::kMoment) {
+      float fc[L::Q];
+#pragma unroll
+      for (int i = 0; i < L::Q; ++i) fc[i] = __fmul_rn(weight<L, float>(i), float(rho));
+      moment::store<L>(fv, n, c, fc);
+      continue;
+    }
 #pragma unroll
     for (int i = 0; i < L::Q; ++i) {
       if constexpr (S::kShifted) {
         const C w = weight<L, float>(i);
         f[i * n + c] = S::save(w * static_cast<C>(rho), w);
-      } else {
+      } else if constexpr (!S::kMoment) {
         // w[spd]*rho in `real` (src/TLBM_Partition.cpp:462-463)
         f[i * n + c] = weight<L, C>(i) * static_cast<C>(rho);
       }
@@ -43,12 +51,23 @@ __global__ void k_init_uniform(DevProblem pb, typename Store<K>::T* f, double rh
 
 // restart: f = feq(u, rho) of each node (load_restart_data, src/TLBM_Partition.cpp:527-532),
 // written to c - e_i so that the first pull returns it at node c
+// the moment-shifted kind: the shift of slot s is formed from node s's own restart fields
+template <class M>
+__device__ __forceinline__ float4 restart_params(const M* ux, const M* uy, const M* uz,
+                                                 const M* rho, int64_t s) {
+  const float r = float(rho[s]);
+  const float r3 = __fmul_rn(3.f, r);
+  return make_float4(r, __fmul_rn(r3, float(ux[s])), __fmul_rn(r3, float(uy[s])),
+                     __fmul_rn(r3, float(uz[s])));
+}
+
 template <class L, int K, class M>
-__global__ void k_init_equilibrium(DevProblem pb, typename Store<K>::T* f, const M* ux,
-                                   const M* uy, const M* uz, const M* rho) {
+__global__ void k_init_equilibrium(DevProblem pb, void* fv, const M* ux, const M* uy,
+                                   const M* uz, const M* rho) {
   using S = Store<K>;
   using C = typename S::C;
   const size_t n = static_cast<size_t>(pb.n);
+  auto* f = static_cast<typename S::P*>(fv);
   TLBM_FOR_CELLS(c, pb.n) {
     int x, y, z;
     decompose(static_cast<int>(c), pb.nx, pb.nxy, x, y, z);
@@ -56,19 +75,30 @@ __global__ void k_init_equilibrium(DevProblem pb, typename Store<K>::T* f, const
     C feq[L::Q];
     ref::equilibrium<L, C>(static_cast<C>(ux[c]), static_cast<C>(uy[c]), static_cast<C>(uz[c]),
                            static_cast<C>(rho[c]), feq);
+    if constexpr (S::kMoment) {
+      moment::params(fv, L::Q, n)[c] = restart_params(ux, uy, uz, rho, c);
 #pragma unroll
-    for (int i = 0; i < L::Q; ++i) {
-      const C w = S::kShifted ? weight<L, float>(i) : C(0);
-      f[i * n + nb.from<L>(i)] = S::save(feq[i], w);
+      for (int i = 0; i < L::Q; ++i) {
+        const int s = nb.from<L>(i);
+        const float sh = moment::shift<L>(i, restart_params(ux, uy, uz, rho, s));
+        f[i * n + s] = __float2bfloat16_rn(__fsub_rn(feq[i], sh));
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < L::Q; ++i) {
+        const C w = S::kShifted ? weight<L, float>(i) : C(0);
+        f[i * n + nb.from<L>(i)] = S::save(feq[i], w);
+      }
     }
   }
 }
 
 template <class L, int K, class O>
-__global__ void k_to_aos(DevProblem pb, const typename Store<K>::T* f, int post_stream, O* out) {
+__global__ void k_to_aos(DevProblem pb, const void* fv, int post_stream, O* out) {
   using S = Store<K>;
   using C = typename S::C;
   const size_t n = static_cast<size_t>(pb.n);
+  const auto* f = static_cast<const typename S::P*>(fv);
   TLBM_FOR_CELLS(c, pb.n) {
     int x, y, z;
     decompose(static_cast<int>(c), pb.nx, pb.nxy, x, y, z);
@@ -76,8 +106,13 @@ __global__ void k_to_aos(DevProblem pb, const typename Store<K>::T* f, int post_
 #pragma unroll
     for (int i = 0; i < L::Q; ++i) {
       const int src = post_stream ? nb.from<L>(i) : static_cast<int>(c);
-      const C w = S::kShifted ? weight<L, float>(i) : C(0);
-      out[c * L::Q + i] = static_cast<O>(S::load(f[i * n + src], w));
+      if constexpr (S::kMoment) {
+        out[c * L::Q + i] = static_cast<O>(
+            moment::load<L>(f, moment::params(fv, L::Q, n), n, i, src));
+      } else {
+        const C w = S::kShifted ? weight<L, float>(i) : C(0);
+        out[c * L::Q + i] = static_cast<O>(S::load(f[i * n + src], w));
+      }
     }
   }
 }
@@ -111,17 +146,19 @@ __device__ double block_sum(double v) {
 }
 
 template <class L, int K>
-__global__ void __launch_bounds__(kThreads) k_mass_partial(DevProblem pb,
-                                                           const typename Store<K>::T* f,
+__global__ void __launch_bounds__(kThreads) k_mass_partial(DevProblem pb, const void* fv,
                                                            double* partial) {
   using S = Store<K>;
   const size_t n = static_cast<size_t>(pb.n);
+  const auto* f = static_cast<const typename S::P*>(fv);
   double acc = 0.0;
   TLBM_FOR_CELLS(c, pb.n) {
     double cell = 0.0;
 #pragma unroll
     for (int i = 0; i < L::Q; ++i) {
-      if constexpr (S::kShifted)
+      if constexpr (S::kMoment)
+        cell += static_cast<double>(moment::load<L>(f, moment::params(fv, L::Q, n), n, i, c));
+      else if constexpr (S::kShifted)
         cell += static_cast<double>(weight<L, float>(i)) + static_cast<double>(f[i * n + c]);
       else
         cell += static_cast<double>(f[i * n + c]);
@@ -153,6 +190,7 @@ cudaError_t by_q_store(int q, int store, A&&... a) {
   TLBM_CASE_K(15, kStoreF16) TLBM_CASE_K(19, kStoreF64) TLBM_CASE_K(19, kStoreF32)
   TLBM_CASE_K(19, kStoreBF16) TLBM_CASE_K(19, kStoreF16) TLBM_CASE_K(27, kStoreF64)
   TLBM_CASE_K(27, kStoreF32) TLBM_CASE_K(27, kStoreBF16) TLBM_CASE_K(27, kStoreF16)
+  TLBM_CASE_K(15, kStoreBF16M) TLBM_CASE_K(19, kStoreBF16M) TLBM_CASE_K(27, kStoreBF16M)
 #undef TLBM_CASE_K
   return cudaErrorInvalidValue;
 }
@@ -160,8 +198,7 @@ cudaError_t by_q_store(int q, int store, A&&... a) {
 template <class L, int K>
 struct InitUniform {
   static cudaError_t run(const DevProblem& pb, void* f, double rho, const Launch& l) {
-    k_init_uniform<L, K><<<blocks_for(pb.n), kThreads, 0, l.stream>>>(
-        pb, static_cast<typename Store<K>::T*>(f), rho);
+    k_init_uniform<L, K><<<blocks_for(pb.n), kThreads, 0, l.stream>>>(pb, f, rho);
     return cudaGetLastError();
   }
 };
@@ -170,7 +207,7 @@ template <class L, int K>
 struct InitEq {
   static cudaError_t run(const DevProblem& pb, void* f, const void* const* m, int mb,
                          const Launch& l) {
-    auto* ff = static_cast<typename Store<K>::T*>(f);
+    void* ff = f;
     if (mb == 8)
       k_init_equilibrium<L, K, double><<<blocks_for(pb.n), kThreads, 0, l.stream>>>(
           pb, ff, static_cast<const double*>(m[0]), static_cast<const double*>(m[1]),
@@ -187,7 +224,7 @@ template <class L, int K>
 struct ToAos {
   static cudaError_t run(const DevProblem& pb, const void* f, int post, void* out, int ob,
                          const Launch& l) {
-    auto* ff = static_cast<const typename Store<K>::T*>(f);
+    const void* ff = f;
     if (ob == 8)
       k_to_aos<L, K, double><<<blocks_for(pb.n), kThreads, 0, l.stream>>>(
           pb, ff, post, static_cast<double*>(out));
@@ -202,8 +239,7 @@ template <class L, int K>
 struct Mass {
   static cudaError_t run(const DevProblem& pb, const void* f, double* partial, int nb,
                          double* out, const Launch& l) {
-    k_mass_partial<L, K><<<nb, kThreads, 0, l.stream>>>(
-        pb, static_cast<const typename Store<K>::T*>(f), partial);
+    k_mass_partial<L, K><<<nb, kThreads, 0, l.stream>>>(pb, f, partial);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_mass_final<<<1, kThreads, 0, l.stream>>>(partial, nb, out);

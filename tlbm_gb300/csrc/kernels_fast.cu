@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(128, kMlpMinBlocks<K>)
 
 template <class L, int K>
 __global__ void __launch_bounds__(128) k_macros_fast(DevProblem pb,
-                                                    const typename Store<K>::T* __restrict__ src,
+                                                    const void* __restrict__ src,
                                                     typename Store<K>::C* ux_o,
                                                     typename Store<K>::C* uy_o,
                                                     typename Store<K>::C* uz_o,
@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(128) k_macros_fast(DevProblem pb,
 }
 
 template <class L, int K>
-__global__ void k_quirk_fast(DevProblem pb, const typename Store<K>::T* __restrict__ src,
+__global__ void k_quirk_fast(DevProblem pb, const void* __restrict__ src,
                              typename Store<K>::C* uy_out) {
   using C = typename Store<K>::C;
   const int c = threadIdx.x;
@@ -164,7 +164,7 @@ __global__ void k_quirk_fast(DevProblem pb, const typename Store<K>::T* __restri
 
 template <class L, int K>
 __global__ void __launch_bounds__(128) k_force_fast(DevProblem pb,
-                                                   const typename Store<K>::T* __restrict__ f,
+                                                   const void* __restrict__ fv,
                                                    typename Store<K>::C* fx_o,
                                                    typename Store<K>::C* fy_o,
                                                    typename Store<K>::C* fz_o) {
@@ -177,6 +177,14 @@ __global__ void __launch_bounds__(128) k_force_fast(DevProblem pb,
   const Nbr nb(x, y, z, pb.nx, pb.ny, pb.nz, pb.nxy);
   const int c = nb.self();
   const size_t n = static_cast<size_t>(pb.n);
+  const auto* f = static_cast<const typename S::P*>(fv);
+  // post-stream value of speed i at cell d: the slot (i, from) of the buffer
+  auto pulled = [&](int i, int from) -> C {
+    if constexpr (S::kMoment)
+      return moment::load<L>(f, moment::params(fv, L::Q, n), n, i, from);
+    else
+      return S::load(f[i * n + from], fast::wgt<L, C>(i));
+  };
   C fx = 0, fy = 0, fz = 0;
   if (pb.nd_type[c] == kSolid) {
 #pragma unroll
@@ -187,8 +195,8 @@ __global__ void __launch_bounds__(128) k_force_fast(DevProblem pb,
       int gx, gy, gz;
       decompose(g, pb.nx, pb.nxy, gx, gy, gz);
       const Nbr ng(gx, gy, gz, pb.nx, pb.ny, pb.nz, pb.nxy);
-      const C f1 = S::load(f[i * n + nb.from<L>(i)], fast::wgt<L, C>(i));
-      const C f2 = S::load(f[b * n + ng.from<L>(b)], fast::wgt<L, C>(b));
+      const C f1 = pulled(i, nb.from<L>(i));
+      const C f2 = pulled(b, ng.from<L>(b));
       const C s = f1 + f2;
       fx += C(L::ex(b)) * s;
       fy += C(L::ey(b)) * s;
@@ -225,7 +233,7 @@ cudaError_t macros_lk(const DevProblem& pb, const void* src, void* const out[4],
   using C = typename Store<K>::C;
   const dim3 g = grid_of(pb, l), b(l.bx, l.by, 1);
   k_macros_fast<L, K><<<g, b, 0, l.stream>>>(
-      pb, static_cast<const typename Store<K>::T*>(src), static_cast<C*>(out[0]),
+      pb, src, static_cast<C*>(out[0]),
       static_cast<C*>(out[1]), static_cast<C*>(out[2]), static_cast<C*>(out[3]));
   return cudaGetLastError();
 }
@@ -233,7 +241,7 @@ cudaError_t macros_lk(const DevProblem& pb, const void* src, void* const out[4],
 template <class L, int K>
 cudaError_t quirk_lk(const DevProblem& pb, const void* src, void* out, const Launch& l) {
   using C = typename Store<K>::C;
-  k_quirk_fast<L, K><<<1, 32, 0, l.stream>>>(pb, static_cast<const typename Store<K>::T*>(src),
+  k_quirk_fast<L, K><<<1, 32, 0, l.stream>>>(pb, src,
                                               static_cast<C*>(out));
   return cudaGetLastError();
 }
@@ -242,7 +250,7 @@ template <class L, int K>
 cudaError_t force_lk(const DevProblem& pb, const void* f, void* const out[3], const Launch& l) {
   using C = typename Store<K>::C;
   const dim3 g = grid_of(pb, l), b(l.bx, l.by, 1);
-  k_force_fast<L, K><<<g, b, 0, l.stream>>>(pb, static_cast<const typename Store<K>::T*>(f),
+  k_force_fast<L, K><<<g, b, 0, l.stream>>>(pb, f,
                                              static_cast<C*>(out[0]), static_cast<C*>(out[1]),
                                              static_cast<C*>(out[2]));
   return cudaGetLastError();
@@ -263,6 +271,9 @@ cudaError_t force_lk(const DevProblem& pb, const void* f, void* const out[3], co
       case 271: return FN<Lattice<27>, kStoreF32>(__VA_ARGS__);                     \
       case 272: return FN<Lattice<27>, kStoreBF16>(__VA_ARGS__);                    \
       case 273: return FN<Lattice<27>, kStoreF16>(__VA_ARGS__);                     \
+      case 154: return FN<Lattice<15>, kStoreBF16M>(__VA_ARGS__);                   \
+      case 194: return FN<Lattice<19>, kStoreBF16M>(__VA_ARGS__);                   \
+      case 274: return FN<Lattice<27>, kStoreBF16M>(__VA_ARGS__);                   \
       default: return cudaErrorInvalidValue;                                        \
     }                                                                               \
   } while (0)

@@ -18,11 +18,20 @@
 
 namespace tlbm {
 
+// the Q values a cell pulls from the buffer `src` (the moment-shifted kind: reconstructed)
 template <class L, int K>
-__device__ __forceinline__ void load_cell(const typename Store<K>::T* __restrict__ src, size_t n,
-                                          const Nbr& nb, typename Store<K>::T (&raw)[L::Q]) {
+__device__ __forceinline__ void load_cell(const void* __restrict__ src, size_t n, const Nbr& nb,
+                                          typename Store<K>::T (&raw)[L::Q]) {
+  using S = Store<K>;
+  const auto* p = static_cast<const typename S::P*>(src);
+  if constexpr (S::kMoment) {
+    const float4* prm = moment::params(src, L::Q, n);
 #pragma unroll
-  for (int i = 0; i < L::Q; ++i) raw[i] = __ldg(src + i * n + nb.from<L>(i));
+    for (int i = 0; i < L::Q; ++i) raw[i] = moment::load<L>(p, prm, n, i, nb.from<L>(i));
+  } else {
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) raw[i] = __ldg(p + i * n + nb.from<L>(i));
+  }
 }
 
 template <class L, int K>
@@ -58,18 +67,28 @@ __device__ __forceinline__ void node_macros(uint8_t t, const C (&f)[L::Q], C u_b
 template <class L, int K>
 __device__ __forceinline__ void load_raw(const StepArgs& a, int x, int y, int z, int c,
                                          typename Store<K>::T (&raw)[L::Q]) {
-  using T = typename Store<K>::T;
+  using S = Store<K>;
+  using P = typename S::P;
   const DevProblem& pb = a.pb;
-  const T* __restrict__ src = static_cast<const T*>(a.src);
+  const P* __restrict__ src = static_cast<const P*>(a.src);
   if (x > 0 && x < pb.nx - 1 && y > 0 && y < pb.ny - 1 && z > 0 && z < pb.nz - 1) {
     // interior cell: speed i comes from a fixed byte offset of the cell's own slot
     const char* base = reinterpret_cast<const char*>(src + c);
+    if constexpr (S::kMoment) {
+      // and its shift from the float4 of the cell it comes from, c - e_i
+      const float4* prm = moment::params(a.src, L::Q, static_cast<size_t>(pb.n)) + c;
 #pragma unroll
-    for (int i = 0; i < L::Q; ++i)
-      raw[i] = __ldg(reinterpret_cast<const T*>(base + pb.pull_off[i]));
+      for (int i = 0; i < L::Q; ++i)
+        raw[i] = __fadd_rn(moment::shift<L>(i, __ldg(prm - pb.pull_cell[i])),
+                           __bfloat162float(__ldg(reinterpret_cast<const P*>(base + pb.pull_off[i]))));
+    } else {
+#pragma unroll
+      for (int i = 0; i < L::Q; ++i)
+        raw[i] = __ldg(reinterpret_cast<const P*>(base + pb.pull_off[i]));
+    }
   } else {
     const Nbr nb(x, y, z, pb.nx, pb.ny, pb.nz, pb.nxy);
-    load_cell<L, K>(src, static_cast<size_t>(pb.n), nb, raw);
+    load_cell<L, K>(a.src, static_cast<size_t>(pb.n), nb, raw);
   }
 }
 
@@ -78,10 +97,14 @@ __device__ __forceinline__ void store_cell(const StepArgs& a, int c,
                                            const typename Store<K>::C (&f)[L::Q]) {
   using S = Store<K>;
   using C = typename S::C;
-  typename S::T* __restrict__ dst = static_cast<typename S::T*>(a.dst);
   const size_t n = static_cast<size_t>(a.pb.n);
+  if constexpr (S::kMoment) {
+    moment::store<L>(a.dst, n, c, f);
+  } else {
+    typename S::P* __restrict__ dst = static_cast<typename S::P*>(a.dst);
 #pragma unroll
-  for (int i = 0; i < L::Q; ++i) dst[i * n + c] = S::save(f[i], fast::wgt<L, C>(i));
+    for (int i = 0; i < L::Q; ++i) dst[i * n + c] = S::save(f[i], fast::wgt<L, C>(i));
+  }
 }
 
 // every node type but fluid: solid bounce-back, inlet/outlet reconstruction and relaxation,
@@ -98,10 +121,17 @@ __device__ __forceinline__ void boundary_node(const StepArgs& a, int x, int y, i
   using C = typename S::C;
   const DevProblem& pb = a.pb;
   if (t == kSolid) {
-    typename S::T* __restrict__ dst = static_cast<typename S::T*>(a.dst);
-    const size_t n = static_cast<size_t>(pb.n);
+    if constexpr (S::kMoment) {
+      float sw[L::Q];
 #pragma unroll
-    for (int i = 0; i < L::Q; ++i) dst[i * n + c] = raw[L::bb(i)];
+      for (int i = 0; i < L::Q; ++i) sw[i] = raw[L::bb(i)];
+      store_cell<L, K>(a, c, sw);
+    } else {
+      typename S::P* __restrict__ dst = static_cast<typename S::P*>(a.dst);
+      const size_t n = static_cast<size_t>(pb.n);
+#pragma unroll
+      for (int i = 0; i < L::Q; ++i) dst[i * n + c] = raw[L::bb(i)];
+    }
     if (a.time_avg) {
       C f[L::Q];
       unpack<L, K>(raw, f);

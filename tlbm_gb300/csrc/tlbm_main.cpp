@@ -39,6 +39,7 @@ int main(int argc, char* argv[]) {
       else if (v == "f32") opt.precision = TLBM_PREC_F32;
       else if (v == "bf16") { opt.precision = TLBM_PREC_BF16; opt.arithmetic = TLBM_ARITH_FAST; }
       else if (v == "f16") { opt.precision = TLBM_PREC_F16; opt.arithmetic = TLBM_ARITH_FAST; }
+      else if (v == "bf16m") { opt.precision = TLBM_PREC_BF16M; opt.arithmetic = TLBM_ARITH_FAST; }
       else { std::fprintf(stderr, "unknown precision %s\n", v.c_str()); return 2; }
     } else if (a == "--arithmetic" && i + 1 < argc) {
       std::string v = argv[++i];

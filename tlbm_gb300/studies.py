@@ -25,6 +25,7 @@ FORMS = {
     "f32": ("f32", "fast"),
     "f16": ("f16", "fast"),
     "bf16": ("bf16", "fast"),
+    "bf16m": ("bf16m", "fast"),
 }
 
 
@@ -65,7 +66,8 @@ def compare(res: dict, ref: dict, geom) -> dict:
             "finite": bool(np.isfinite(res["ux"]).all())}
 
 
-def precision_study(geom, params, steps: int, forms=("f64-fast", "f32", "f16", "bf16"),
+def precision_study(geom, params, steps: int,
+                    forms=("f64-fast", "f32", "f16", "bf16", "bf16m"),
                     reference: str = "f64-reference", device: int = 0) -> dict:
     """Run every form and the reference form; returns per-form errors, MLUPS and mass drift."""
     ref = run_form(geom, params, reference, steps, device)
