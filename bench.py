@@ -308,7 +308,8 @@ def run_ours(args, dist):
             "re": 200.0,
             "u_in": 0.04,
             "omega": round(p.omega, 6),
-            "l2": "populations (%.1f GB) larger than L2; no flush" % (2 * q * sb * n / 1e9),
+            "l2": "populations (%.1f GB) larger than L2; no flush" % (
+                n * (cell_bytes(q, args.precision) - 1) / 1e9),
             "parallelism": "replicas only" if dist.world > 1 else "single GPU",
         },
         "roofline": {
