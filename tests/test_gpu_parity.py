@@ -312,5 +312,8 @@ def test_bf16m_restart_and_steps_close_to_f32(q):
     # writer and reader would leave no gain at all
     assert rms(d_m) < rms(d_b) / 2
     assert np.abs(d_m).max() < np.abs(d_b).max()
-    for a, b in zip(out["bf16m"][1], out["f32"][1]):
-        assert np.abs(np.asarray(a, np.float64) - b).max() <= 1e-4
+    for k in range(4):  # ux, uy, uz, rho: closer to FP32 than BF16 storage of f - w
+        ref = np.asarray(out["f32"][1][k], np.float64)
+        e_m = np.abs(np.asarray(out["bf16m"][1][k], np.float64) - ref)
+        e_b = np.abs(np.asarray(out["bf16"][1][k], np.float64) - ref)
+        assert e_m.max() <= 5e-4 and rms(e_m) < rms(e_b), k
