@@ -77,14 +77,21 @@ typedef struct tlbm_options {
   int rbgk;        /* 1: params.lbm dynamics 2 ("RBGK", include/Problem.h:19) runs the
                       regularised BGK collision (fast arithmetic only); 0: the reference's
                       behaviour, streaming without relaxation */
-  int reserved[8];
+  int mrt;         /* 1: params.lbm dynamics 3 ("MRT", include/Problem.h:19; no case in the
+                      reference, which streams without relaxation) runs the two-rate
+                      moment-space collision: stress moments at omega, moments above second
+                      order at mrt_ghost_rate (fast arithmetic only) */
+  float mrt_ghost_rate; /* ghost-moment rate in (0, 2); <= 0 selects 1.2.  The rate omega
+                           gives BGK, 1 the regularised collision. */
+  int reserved[6];
 } tlbm_options;
 
 /* The 23 values of params.lbm in file order (Problem, include/Problem.h:18-40). */
 typedef struct tlbm_problem {
   char lattice[8]; /* "D3Q15" | "D3Q19" | "D3Q27" */
-  int dynamics;    /* 1 = LBGK, 2 = stream without relaxation (reference behaviour) or, with
-                      tlbm_options.rbgk, regularised BGK */
+  int dynamics;    /* 1 = LBGK; 2 = stream without relaxation (reference behaviour) or, with
+                      tlbm_options.rbgk, regularised BGK; 3 = stream without relaxation or,
+                      with tlbm_options.mrt, the two-rate moment-space collision */
   int num_ts, ts_rep_freq, warmup_ts, plot_freq;
   double cs, rho_lbm, u_lbm, omega;
   int nx, ny, nz;
@@ -104,7 +111,8 @@ void tlbm_default_options(tlbm_options* opt);
  * process drives the whole lattice); `size` must exceed the largest partition id, as the
  * reference requires (src/TLBM_Partition.cpp:218-224).  Options: defaults, overridden by an
  * optional `tlbm.cfg` in workdir (lines `key value`: precision f64|f32|bf16|f16,
- * arithmetic reference|fast, block_x N, block_y N, device N, rbgk 0|1). */
+ * arithmetic reference|fast, block_x N, block_y N, device N, rbgk 0|1, mrt 0|1,
+ * mrt_ghost_rate X). */
 tlbm_status tlbm_create(const char* workdir, int rank, int size, tlbm_handle** out);
 
 /* As tlbm_create with explicit options (tlbm.cfg is not read). */

@@ -44,7 +44,8 @@ class Options(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_int), ("precision", ctypes.c_int),
                 ("arithmetic", ctypes.c_int), ("closure", ctypes.c_int),
                 ("block_x", ctypes.c_int), ("block_y", ctypes.c_int), ("device", ctypes.c_int),
-                ("rbgk", ctypes.c_int), ("reserved", ctypes.c_int * 8)]
+                ("rbgk", ctypes.c_int), ("mrt", ctypes.c_int), ("mrt_ghost_rate", ctypes.c_float),
+                ("reserved", ctypes.c_int * 6)]
 
 
 class Problem(ctypes.Structure):
@@ -150,7 +151,7 @@ def declared_symbols(header: str = HEADER) -> list[str]:
 
 
 def options(precision="f32", arithmetic=None, block_x=0, block_y=0, device=0,
-            rbgk=False) -> Options:
+            rbgk=False, mrt=False, ghost_rate=0.0) -> Options:
     o = Options()
     library().tlbm_default_options(ctypes.byref(o))
     o.precision = PREC[precision]
@@ -159,6 +160,8 @@ def options(precision="f32", arithmetic=None, block_x=0, block_y=0, device=0,
     o.arithmetic = ARITH[arithmetic]
     o.block_x, o.block_y, o.device = block_x, block_y, device
     o.rbgk = int(bool(rbgk))
+    o.mrt = int(bool(mrt))
+    o.mrt_ghost_rate = float(ghost_rate)
     return o
 
 
@@ -175,7 +178,7 @@ class TLBMPartition:
     def __init__(self, workdir: str = ".", rank: int = 0, size: int = 1 << 20,
                  precision: str | None = None, arithmetic: str | None = None,
                  block_x: int = 0, block_y: int = 0, device: int = 0, rbgk: bool = False,
-                 _handle=None):
+                 mrt: bool = False, ghost_rate: float = 0.0, _handle=None):
         self._L = library()
         self._h = ctypes.c_void_p()
         self.workdir = workdir
@@ -185,7 +188,8 @@ class TLBMPartition:
             # like the reference binary: defaults, optionally overridden by workdir/tlbm.cfg
             _check(self._L.tlbm_create(workdir.encode(), rank, size, ctypes.byref(self._h)))
         else:
-            o = options(precision or "f32", arithmetic, block_x, block_y, device, rbgk)
+            o = options(precision or "f32", arithmetic, block_x, block_y, device, rbgk, mrt,
+                        ghost_rate)
             _check(self._L.tlbm_create_ex(workdir.encode(), rank, size, ctypes.byref(o),
                                           ctypes.byref(self._h)))
         try:
@@ -198,11 +202,11 @@ class TLBMPartition:
     @classmethod
     def from_arrays(cls, problem: Problem, nd_type, parts=None, workdir=None,
                     precision="f64", arithmetic=None, block_x=0, block_y=0, device=0,
-                    rbgk=False):
+                    rbgk=False, mrt=False, ghost_rate=0.0):
         L = library()
         nd = np.ascontiguousarray(nd_type, dtype=np.int32)
         pp = None if parts is None else np.ascontiguousarray(parts, dtype=np.int32)
-        o = options(precision, arithmetic, block_x, block_y, device, rbgk)
+        o = options(precision, arithmetic, block_x, block_y, device, rbgk, mrt, ghost_rate)
         h = ctypes.c_void_p()
         _check(L.tlbm_create_from_arrays(ctypes.byref(problem), nd.ctypes.data,
                                          None if pp is None else pp.ctypes.data,

@@ -171,6 +171,10 @@ Status apply_config_file(const std::string& path, tlbm_options* opt) {
       opt->device = std::atoi(val.c_str());
     } else if (key == "rbgk") {
       opt->rbgk = std::atoi(val.c_str()) != 0;
+    } else if (key == "mrt") {
+      opt->mrt = std::atoi(val.c_str()) != 0;
+    } else if (key == "mrt_ghost_rate") {
+      opt->mrt_ghost_rate = static_cast<float>(std::atof(val.c_str()));
     } else {
       return Status::err(TLBM_ERR_INVALID_ARGUMENT, path + ": unknown key " + key);
     }
@@ -295,10 +299,13 @@ Status Engine::init(const int32_t* nd_type, const int32_t* parts, int size) {
   if (ref_arith_ && (store_ == kStoreBF16 || store_ == kStoreF16 || store_ == kStoreBF16M))
     return Status::err(TLBM_ERR_INVALID_ARGUMENT,
                        "16-bit storage has no reference arithmetic; use TLBM_ARITH_FAST");
-  if (opt_.rbgk && ref_arith_)
+  if ((opt_.rbgk || opt_.mrt) && ref_arith_)
     return Status::err(TLBM_ERR_UNSUPPORTED,
-                       "the regularised BGK collision has no reference arithmetic (the reference "
-                       "streams without relaxation for dynamics 2): use TLBM_ARITH_FAST");
+                       "the regularised and moment-space collisions have no reference arithmetic "
+                       "(the reference streams without relaxation for dynamics 2 and 3): use "
+                       "TLBM_ARITH_FAST");
+  if (opt_.mrt && opt_.mrt_ghost_rate >= 2.0f)
+    return Status::err(TLBM_ERR_INVALID_ARGUMENT, "mrt_ghost_rate must lie in (0, 2)");
   if (opt_.closure != TLBM_CLOSURE_PARAMS)
     return Status::err(TLBM_ERR_UNSUPPORTED, "closure option not available");
   sb_ = store_bytes(store_);
@@ -426,7 +433,14 @@ Status Engine::init(const int32_t* nd_type, const int32_t* parts, int size) {
   pb_.u_bc = prob_.u_lbm;
   pb_.rho_bc = prob_.rho_lbm;
   pb_.dynamics = prob_.dynamics;
-  pb_.rbgk = (opt_.rbgk && prob_.dynamics == 2) ? 1 : 0;
+  // moment-space collision: dynamics 2 with rbgk (ghost rate 1), dynamics 3 with mrt
+  pb_.mcoll = 0;
+  pb_.ghost_omega = 1.0;
+  if (opt_.rbgk && prob_.dynamics == 2) pb_.mcoll = 1;
+  if (opt_.mrt && prob_.dynamics == 3) {
+    pb_.mcoll = 1;
+    pb_.ghost_omega = opt_.mrt_ghost_rate > 0.0f ? opt_.mrt_ghost_rate : 1.2;
+  }
   pb_.has_type5 = has_type5_ ? 1 : 0;
   fill_derived(pb_, q_, sb_);
 

@@ -24,7 +24,11 @@ struct DevProblem {
   // thread would spend FP64-pipe slots on it)
   float omega_f, cs_f, u_bc_f, rho_bc_f, nu_f;
   int dynamics;
-  int rbgk;  // dynamics 2 runs the regularised BGK collision (fast arithmetic)
+  // moment-space collision (fast arithmetic): dynamics 2 with the rbgk option (regularised
+  // BGK, ghost rate 1) or dynamics 3 with the mrt option (ghost rate from the options)
+  int mcoll;
+  double ghost_omega;
+  float ghost_omega_f;
   int has_type5;
   // byte offset, from a cell's own population of speed 0, of the population of speed i that an
   // interior cell (no face of the box) pulls: i*n*bytes - (ex + ey*nx + ez*nx*ny)*bytes
@@ -37,7 +41,7 @@ struct DevProblem {
 };
 
 // whether nodes relax: LBGK, or the regularised BGK of dynamics 2
-TLBM_HD bool relaxes(const DevProblem& p) { return p.dynamics == 1 || p.rbgk; }
+TLBM_HD bool relaxes(const DevProblem& p) { return p.dynamics == 1 || p.mcoll; }
 
 // problem parameters in the compute type
 template <class C>
@@ -49,6 +53,7 @@ struct Par<double> {
   static TLBM_HD double u_bc(const DevProblem& p) { return p.u_bc; }
   static TLBM_HD double rho_bc(const DevProblem& p) { return p.rho_bc; }
   static TLBM_HD double nu(const DevProblem& p) { return p.nu; }
+  static TLBM_HD double ghost_omega(const DevProblem& p) { return p.ghost_omega; }
   static TLBM_HD double u_in(const DevProblem& p, int xy) {
     return p.inlet_d ? p.inlet_d[xy] : p.u_bc;
   }
@@ -60,6 +65,7 @@ struct Par<float> {
   static TLBM_HD float u_bc(const DevProblem& p) { return p.u_bc_f; }
   static TLBM_HD float rho_bc(const DevProblem& p) { return p.rho_bc_f; }
   static TLBM_HD float nu(const DevProblem& p) { return p.nu_f; }
+  static TLBM_HD float ghost_omega(const DevProblem& p) { return p.ghost_omega_f; }
   static TLBM_HD float u_in(const DevProblem& p, int xy) {
     return p.inlet_f ? p.inlet_f[xy] : p.u_bc_f;
   }
@@ -86,6 +92,7 @@ inline void fill_derived(DevProblem& pb, int q, int bytes) {
   pb.u_bc_f = static_cast<float>(pb.u_bc);
   pb.rho_bc_f = static_cast<float>(pb.rho_bc);
   pb.nu_f = static_cast<float>(pb.nu);
+  pb.ghost_omega_f = static_cast<float>(pb.ghost_omega);
   if (q == 15) fill_pull_offsets<Lattice<15>>(pb, bytes);
   if (q == 19) fill_pull_offsets<Lattice<19>>(pb, bytes);
   if (q == 27) fill_pull_offsets<Lattice<27>>(pb, bytes);

@@ -75,11 +75,11 @@ __global__ void __launch_bounds__(128, kMlpMinBlocks<K>)
       for (int k = 0; k < 6; ++k) pi[k] = st.pi[k];
       if (relaxes(pb)) fast::closure_inputs<L, C>(st, cl, xin);
     } else {
-      if (pb.cs > 0 && pb.rbgk)
+      if (pb.cs > 0 && pb.mcoll)
         boundary_node<L, K, true, true>(a, x, y, c, t, raw, rho, ux, uy, uz);
       else if (pb.cs > 0)
         boundary_node<L, K, true, false>(a, x, y, c, t, raw, rho, ux, uy, uz);
-      else if (pb.rbgk)
+      else if (pb.mcoll)
         boundary_node<L, K, false, true>(a, x, y, c, t, raw, rho, ux, uy, uz);
       else
         boundary_node<L, K, false, false>(a, x, y, c, t, raw, rho, ux, uy, uz);
@@ -104,10 +104,10 @@ __global__ void __launch_bounds__(128, kMlpMinBlocks<K>)
     fast::fluid_pair_terms<L, C>(st);
     const C omega = fast::closure_omega<C>(net, cl, Par<C>::omega(pb), Par<C>::cs(pb),
                                            Par<C>::nu(pb), q2);
-    if (pb.rbgk) {
+    if (pb.mcoll) {
 #pragma unroll
       for (int k = 0; k < 6; ++k) st.pi[k] = pi[k];
-      fast::fluid_relax_reg<L, C>(f, st, omega);
+      fast::fluid_relax_moment<L, C>(f, st, omega, Par<C>::ghost_omega(pb));
     } else {
       fast::fluid_relax<L, C>(f, st, omega);
     }
@@ -217,11 +217,11 @@ cudaError_t step_lk(const StepArgs& a, const Launch& l) {
   const dim3 g = grid_of(a.pb, l), b(l.bx, l.by, 1);
   if (a.closure)
     k_step_fast_mlp<L, K><<<g, b, 0, l.stream>>>(a, *static_cast<const mlp::Closure*>(a.closure));
-  else if (a.pb.cs > 0 && a.pb.rbgk)
+  else if (a.pb.cs > 0 && a.pb.mcoll)
     k_step_fast<L, K, fast::kClosureSmag, true><<<g, b, 0, l.stream>>>(a);
   else if (a.pb.cs > 0)
     k_step_fast<L, K, fast::kClosureSmag, false><<<g, b, 0, l.stream>>>(a);
-  else if (a.pb.rbgk)
+  else if (a.pb.mcoll)
     k_step_fast<L, K, fast::kClosureNone, true><<<g, b, 0, l.stream>>>(a);
   else
     k_step_fast<L, K, fast::kClosureNone, false><<<g, b, 0, l.stream>>>(a);

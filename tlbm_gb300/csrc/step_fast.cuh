@@ -109,7 +109,7 @@ __device__ __forceinline__ void store_cell(const StepArgs& a, int c,
 
 // every node type but fluid: solid bounce-back, inlet/outlet reconstruction and relaxation,
 // the moving-wall nudge.  kSmag: boundary nodes relax at the Smagorinsky rate; kReg: with the
-// regularised collision.
+// moment-space collision.
 template <class L, int K, bool kSmag, bool kReg>
 __device__ __forceinline__ void boundary_node(const StepArgs& a, int x, int y, int c, uint8_t t,
                                               const typename Store<K>::T (&raw)[L::Q],
@@ -176,7 +176,7 @@ __device__ __forceinline__ void boundary_node(const StepArgs& a, int x, int y, i
     C om = Par<C>::omega(pb);
     if (kSmag) om = fast::smagorinsky_omega<L, C>(f, feq, Par<C>::cs(pb), Par<C>::nu(pb));
     if constexpr (kReg)
-      fast::relax_reg<L, C>(f, feq, om);
+      fast::relax_moment<L, C>(f, feq, om, Par<C>::ghost_omega(pb));
     else
       fast::relax<L, C>(f, feq, om);
   }
@@ -194,7 +194,7 @@ __device__ __forceinline__ void accumulate_avg(const StepArgs& a, int c, C rho, 
 }
 
 // kClosure: fast::kClosureNone (BGK) or kClosureSmag (the learned closure has its own kernel,
-// kernels_fast.cu: k_step_fast_mlp); kReg: regularised collision (dynamics 2 with the option)
+// kernels_fast.cu: k_step_fast_mlp); kReg: the moment-space collision (RBGK / MRT)
 template <class L, int K, int kClosure, bool kReg = false>
 __device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z) {
   using S = Store<K>;
@@ -209,7 +209,8 @@ __device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z
     C f[L::Q];
     unpack<L, K>(raw, f);
     fast::fluid_collide<L, C, kClosure, kReg>(f, Par<C>::omega(pb), Par<C>::cs(pb),
-                                              Par<C>::nu(pb), relaxes(pb), rho, ux, uy, uz);
+                                              Par<C>::nu(pb), Par<C>::ghost_omega(pb),
+                                              relaxes(pb), rho, ux, uy, uz);
     store_cell<L, K>(a, c, f);
   } else {
     boundary_node<L, K, kClosure == fast::kClosureSmag, kReg>(a, x, y, c, t, raw, rho, ux, uy,
