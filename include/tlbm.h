@@ -81,8 +81,8 @@ typedef struct tlbm_options {
                       reference, which streams without relaxation) runs the two-rate
                       moment-space collision: stress moments at omega, moments above second
                       order at mrt_ghost_rate (fast arithmetic only) */
-  float mrt_ghost_rate; /* ghost-moment rate in (0, 2); <= 0 selects 1.2.  The rate omega
-                           gives BGK, 1 the regularised collision. */
+  float mrt_ghost_rate; /* ghost-moment rate in (0, 2), a float; <= 0 selects 1.2.  The rate
+                           omega gives BGK, 1 the regularised collision. */
   int reserved[6];
 } tlbm_options;
 
