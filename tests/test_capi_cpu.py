@@ -166,3 +166,42 @@ def test_python_mirror_raises(lib, tmp_path):
     with pytest.raises(T.TLBMError) as e:
         T.TLBMPartition(str(tmp_path))
     assert e.value.status == T.ERR_IO
+
+
+def _problem(nx, ny, nz, dynamics=1):
+    g = G.sphere_in_box(8, 8, 12, 2, 4, 4, 5)
+    p = G.params_lattice_units(g, "D3Q19", 0.04, 20.0, 4.0, 10)
+    prob = T.problem_from_params(p)
+    prob.nx, prob.ny, prob.nz, prob.dynamics = nx, ny, nz, dynamics
+    return prob
+
+
+def _create(prob, nd, **kw):
+    o = T.options(**kw)
+    h = ctypes.c_void_p()
+    st = T.library().tlbm_create_from_arrays(ctypes.byref(prob), nd.ctypes.data, None, None,
+                                              ctypes.byref(o), ctypes.byref(h))
+    return st, T.library().tlbm_get_last_error(None).decode()
+
+
+@pytest.mark.parametrize("dims,status", [((65536, 65536, 1), T.ERR_UNSUPPORTED),  # >= 2^31 cells
+                                         ((1, 1, 70000), T.ERR_UNSUPPORTED),      # nz > 65535
+                                         ((0, 8, 8), T.ERR_FORMAT)])
+def test_lattice_size_limits(lib, dims, status):
+    """Sizes beyond what one device kernel grid addresses are refused before the node types are
+    read or any memory is allocated (the node-type array here is a single value)."""
+    st, msg = _create(_problem(*dims), np.zeros(1, np.int32), precision="f64")
+    assert st == status and msg
+
+
+@pytest.mark.parametrize("kw,dynamics,status", [
+    ({"precision": "bf16", "arithmetic": "reference"}, 1, T.ERR_INVALID_ARGUMENT),
+    ({"precision": "bf16m", "arithmetic": "reference"}, 1, T.ERR_INVALID_ARGUMENT),
+    ({"precision": "f64", "arithmetic": "reference", "rbgk": True}, 2, T.ERR_UNSUPPORTED),
+    ({"precision": "f64", "arithmetic": "reference", "mrt": True}, 3, T.ERR_UNSUPPORTED),
+    ({"precision": "f64", "arithmetic": "fast", "mrt": True, "ghost_rate": 2.5}, 3,
+     T.ERR_INVALID_ARGUMENT)])
+def test_option_combinations_refused_before_the_device(lib, kw, dynamics, status):
+    nd = np.zeros(8 * 8 * 12, np.int32)
+    st, msg = _create(_problem(8, 8, 12, dynamics), nd, **kw)
+    assert st == status and msg
