@@ -25,37 +25,31 @@ __device__ __forceinline__ void launder(double& v) { asm volatile("" : "+d"(v));
 
 // Learned closure.  The network runs on the tensor cores, one warp (32 cells) at a time
 // (mlp::forward_warp); the closure's description arrives by value in the kernel parameters.
-// The block starts the copy of the network to shared memory, loads and prepares its cells
-// (non-fluid nodes finish here), and only then waits for the copy, so the copy's latency hides
-// behind the cell loads.  Every lane of a warp reaches the warp-collective part, which a warp
-// without fluid cells skips.  Across the network only f, rho, u and Pi:Pi stay live; the pair
-// terms of the equilibrium are recomputed after it.
+// Every lane of a warp reaches the warp-collective part, which a warp without fluid cells
+// skips.  Across the network only f, rho, u and Pi:Pi stay live (and Pi for the regularised
+// collision); the pair terms of the equilibrium are recomputed after it.
 #ifndef TLBM_MLP_MIN_BLOCKS
 #define TLBM_MLP_MIN_BLOCKS 8  // resident blocks per SM: 64 registers per thread
 #endif
 template <int K>
 constexpr int kMlpMinBlocks = K == kStoreF64 ? 4 : TLBM_MLP_MIN_BLOCKS;
 
-template <class L, int K>
-__global__ void __launch_bounds__(128, kMlpMinBlocks<K>)
-    k_step_fast_mlp(StepArgs a, const mlp::Closure cl) {
+// One cell of the learned-closure step; all 32 lanes of the warp call it together (the network
+// is warp-collective), lanes outside the lattice included.  kReg: regularised (moment-space)
+// collision, which also needs the stress after the network.
+template <class L, int K, bool kReg>
+__device__ __forceinline__ void mlp_cell(const StepArgs& a, const mlp::Closure& cl,
+                                         const mlp::MmaWeights& sw, uint4* xs, float* ys, int x,
+                                         int y, int z, int lane) {
   using S = Store<K>;
   using C = typename S::C;
-  __shared__ mlp::MmaWeights sw;
-  __shared__ uint4 xs[4][32];
-  __shared__ float ys[4][32];
-  const int tid = threadIdx.x + threadIdx.y * blockDim.x;
-  mlp::copy_mma_weights(cl.w, sw, tid, blockDim.x * blockDim.y);
   const DevProblem& pb = a.pb;
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  const int z = blockIdx.z;
   const bool in = x < pb.nx && y < pb.ny;
   const int c = x + y * pb.nx + z * pb.nxy;
   bool fluid = false;
   C f[L::Q];
   C rho = 0, ux = 0, uy = 0, uz = 0, q2 = 0;
-  C pi[6];  // kept across the network only for the regularised collision
+  C pi[kReg ? 6 : 1];
   float xin[mlp::kIn] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   if (in) {
     typename S::T raw[L::Q];
@@ -71,26 +65,23 @@ __global__ void __launch_bounds__(128, kMlpMinBlocks<K>)
       uy = st.uy;
       uz = st.uz;
       q2 = st.q2;
+      if constexpr (kReg) {
 #pragma unroll
-      for (int k = 0; k < 6; ++k) pi[k] = st.pi[k];
+        for (int k = 0; k < 6; ++k) pi[k] = st.pi[k];
+      }
       if (relaxes(pb)) fast::closure_inputs<L, C>(st, cl, xin);
     } else {
-      if (pb.cs > 0 && pb.mcoll)
-        boundary_node<L, K, true, true>(a, x, y, c, t, raw, rho, ux, uy, uz);
-      else if (pb.cs > 0)
-        boundary_node<L, K, true, false>(a, x, y, c, t, raw, rho, ux, uy, uz);
-      else if (pb.mcoll)
-        boundary_node<L, K, false, true>(a, x, y, c, t, raw, rho, ux, uy, uz);
+      if (pb.cs > 0)
+        boundary_node<L, K, true, kReg>(a, x, y, c, t, raw, rho, ux, uy, uz);
       else
-        boundary_node<L, K, false, false>(a, x, y, c, t, raw, rho, ux, uy, uz);
+        boundary_node<L, K, false, kReg>(a, x, y, c, t, raw, rho, ux, uy, uz);
       if (a.time_avg) accumulate_avg<C>(a, c, rho, ux, uy, uz);
     }
   }
   __syncthreads();  // the network is in shared memory
-  const int warp = tid >> 5, lane = tid & 31;
   float net = 0.f;
   if (__any_sync(0xFFFFFFFFu, fluid && relaxes(pb)))
-    net = mlp::forward_warp(sw, xs[warp], ys[warp], xin, lane);
+    net = mlp::forward_warp(sw, xs, ys, xin, lane);
   if (!fluid) return;
   if (relaxes(pb)) {
     launder(ux);
@@ -104,7 +95,7 @@ __global__ void __launch_bounds__(128, kMlpMinBlocks<K>)
     fast::fluid_pair_terms<L, C>(st);
     const C omega = fast::closure_omega<C>(net, cl, Par<C>::omega(pb), Par<C>::cs(pb),
                                            Par<C>::nu(pb), q2);
-    if (pb.mcoll) {
+    if constexpr (kReg) {
 #pragma unroll
       for (int k = 0; k < 6; ++k) st.pi[k] = pi[k];
       fast::fluid_relax_moment<L, C>(f, st, omega, Par<C>::ghost_omega(pb));
@@ -114,6 +105,22 @@ __global__ void __launch_bounds__(128, kMlpMinBlocks<K>)
   }
   store_cell<L, K>(a, c, f);
   if (a.time_avg) accumulate_avg<C>(a, c, rho, ux, uy, uz);
+}
+
+// The learned-closure step: one thread per cell like k_step_fast.  The block copies the network
+// image to shared memory while its cells load, and waits for the copy only before the network.
+template <class L, int K, bool kReg>
+__global__ void __launch_bounds__(128, kMlpMinBlocks<K>)
+    k_step_fast_mlp(StepArgs a, const mlp::Closure cl) {
+  __shared__ mlp::MmaWeights sw;
+  __shared__ uint4 xs[4][32];
+  __shared__ float ys[4][32];
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+  mlp::copy_mma_weights(cl.w, sw, tid, blockDim.x * blockDim.y);
+  const int warp = tid >> 5, lane = tid & 31;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  mlp_cell<L, K, kReg>(a, cl, sw, xs[warp], ys[warp], x, y, blockIdx.z, lane);
 }
 
 template <class L, int K>
@@ -215,9 +222,13 @@ dim3 grid_of(const DevProblem& pb, const Launch& l) {
 template <class L, int K>
 cudaError_t step_lk(const StepArgs& a, const Launch& l) {
   const dim3 g = grid_of(a.pb, l), b(l.bx, l.by, 1);
-  if (a.closure)
-    k_step_fast_mlp<L, K><<<g, b, 0, l.stream>>>(a, *static_cast<const mlp::Closure*>(a.closure));
-  else if (a.pb.cs > 0 && a.pb.mcoll)
+  if (a.closure) {
+    const mlp::Closure& cl = *static_cast<const mlp::Closure*>(a.closure);
+    if (a.pb.mcoll)
+      k_step_fast_mlp<L, K, true><<<g, b, 0, l.stream>>>(a, cl);
+    else
+      k_step_fast_mlp<L, K, false><<<g, b, 0, l.stream>>>(a, cl);
+  } else if (a.pb.cs > 0 && a.pb.mcoll)
     k_step_fast<L, K, fast::kClosureSmag, true><<<g, b, 0, l.stream>>>(a);
   else if (a.pb.cs > 0)
     k_step_fast<L, K, fast::kClosureSmag, false><<<g, b, 0, l.stream>>>(a);

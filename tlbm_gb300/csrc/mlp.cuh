@@ -17,9 +17,10 @@
 
 #include <cuda_bf16.h>
 
+#include <cstddef>
 #include <cstdint>
-
 #include <cstring>
+#include <type_traits>
 
 namespace tlbm {
 namespace mlp {
@@ -92,54 +93,92 @@ __device__ __forceinline__ float act(float z) {
 
 // ---------------------------------------------------------------- tensor-core forward pass
 // Inference inside the collide kernel runs on the tensor cores one warp at a time: the warp's
-// 32 cells form two 16-row tiles, and mma.sync m16n8k16 (BF16 in, FP32 accumulate) computes
-//   layer 1: H1[32 x 32] = X[32 x 16] W1^T  (K padded from 8 to 16 with zeros), 8 MMAs
-//   layer 2: H2[32 x 32] = act(H1) W2^T,                                        16 MMAs
-//   layer 3: y[32]       = act(H2) w3,                                           4 MMAs
+// 32 cells form two 16-row tiles, and mma.sync (BF16 in, FP32 accumulate) computes
+//   layer 1: H1[32 x 32] = X[32 x 8] W1^T + b1,  m16n8k8,   8 MMAs
+//   layer 2: H2[32 x 32] = act(H1) W2^T + b2,    m16n8k16, 16 MMAs
+//   layer 3: y[32]       = act(H2) w3 + b3,      m16n8k16,  4 MMAs
 // The FP32 accumulator fragment of layer 1 has the layout of the BF16 A fragment of layer 2
 // (rows g, g+8; columns 2t, 2t+1 of each 8-column tile), so act(H1) is packed to BF16 in
 // registers and fed back without a trip through shared memory; layer 3 (32 -> 1) is one more
 // pair of MMAs with w3 as column 0 of the B tile.
 
-constexpr int kRowStride = 40;  // BF16 row stride of the 32-column tiles: ldmatrix rows hit
-                                // 32 distinct banks (80-byte rows)
-
-// The network as the tensor-core pass reads it, built on the host (build_mma_weights) and
-// copied to shared memory with 16-byte loads.  Matrices are stored [output][input] (the
-// col-major B operand of mma.m16n8k16), so ldmatrix hands out B fragments directly; w3 is
-// row 0 of an otherwise zero 8-row tile (column 0 of the layer-3 B tile).
+// The network as the tensor-core pass reads it: every lane's B fragments, in fragment order,
+// so one 16-byte load hands a lane four fragment registers.  Lane (g, t) = (lane / 4, lane % 4)
+// holds, for column tile n (hidden units 8n .. 8n + 7):
+//   layer 1 (K = 8):  w1f[lane].n    = (W1[8n+g][2t], W1[8n+g][2t+1])
+//   layer 2 (K = 32): w2f[n][lane].j = (W2[8n+g][8j+2t], W2[8n+g][8j+2t+1]), j = 0..3
+//                     (j = 0, 1: the k16 step over inputs 0..15; j = 2, 3: inputs 16..31)
+//   layer 3 (N = 1):  w3 is column 0 of the B tile: lanes with g = 0 hold w3f[t] = the pairs
+//                     w3[2t..], w3[8+2t..], w3[16+2t..], w3[24+2t..]; the others the zero row
+//                     w3f[4]
+// and the biases as accumulator quads, bNq[n][t] = (bN[8n+2t], bN[8n+2t+1]) twice: the initial
+// value of the fragment (rows g, g+8; columns 2t, 2t+1) of column tile n, loaded straight into
+// the MMA's C operand.  Matrices W are [output][input]; weights are BF16 bits, biases FP32.
+// Both the collide kernel and the training pass read the image from shared memory.
 struct alignas(16) MmaWeights {
-  uint16_t w1[kHid][kIn];          // BF16 bits, 16-byte rows
-  uint16_t w2[kHid][kRowStride];   // BF16 bits, columns 32..39 unused
-  uint16_t w3[8][kRowStride];      // row 0 = w3, rows 1..7 = 0
-  float b1[kHid], b2[kHid];
-  float b3;
+  uint4 w1f[32];      // [lane]
+  uint4 w2f[4][32];   // [n][lane]
+  float4 b1q[4][4];   // [n][t]
+  float4 b2q[4][4];   // [n][t]
+  uint4 w3f[5];       // [t], row 4 = 0
+  float b3, pad[3];
 };
 static_assert(sizeof(MmaWeights) % 16 == 0, "copied as 16-byte words");
 
-inline void build_mma_weights(const float* params, MmaWeights* out) {
-  memset(out, 0, sizeof(*out));
-  for (int j = 0; j < kHid; ++j) {
-    for (int k = 0; k < kIn; ++k) out->w1[j][k] = bf16_bits_host(params[oW1 + j * kIn + k]);
-    for (int k = 0; k < kHid; ++k) out->w2[j][k] = bf16_bits_host(params[oW2 + j * kHid + k]);
-    out->w3[0][j] = bf16_bits_host(params[oW3 + j]);
-    out->b1[j] = params[oB1 + j];
-    out->b2[j] = params[oB2 + j];
+// the image from kParams FP32 parameters (weights rounded to BF16 here); bits(v) gives the
+// BF16 bits of v, so host and device build the same image
+template <class Bits>
+__host__ __device__ inline void mma_image_entry(const float* p, int k, MmaWeights& o, Bits bits) {
+  auto pair = [&](int i) {  // p[i], p[i + 1] as one fragment word (p[i] in the low half)
+    return static_cast<uint32_t>(bits(p[i])) | (static_cast<uint32_t>(bits(p[i + 1])) << 16);
+  };
+  // k enumerates the 16-byte words of the image
+  if (k < 32) {
+    const int g = k >> 2, t = k & 3;
+    uint32_t r[4];
+    for (int n = 0; n < 4; ++n) r[n] = pair(oW1 + (8 * n + g) * kIn + 2 * t);
+    o.w1f[k] = {r[0], r[1], r[2], r[3]};
+  } else if (k < 32 + 128) {
+    const int n = (k - 32) >> 5, lane = (k - 32) & 31, g = lane >> 2, t = lane & 3;
+    uint32_t r[4];
+    for (int j = 0; j < 4; ++j) r[j] = pair(oW2 + (8 * n + g) * kHid + 8 * j + 2 * t);
+    o.w2f[n][lane] = {r[0], r[1], r[2], r[3]};
+  } else if (k < 160 + 16) {
+    const int n = (k - 160) >> 2, t = (k - 160) & 3;
+    const float* b = p + oB1 + 8 * n + 2 * t;
+    o.b1q[n][t] = {b[0], b[1], b[0], b[1]};
+  } else if (k < 176 + 16) {
+    const int n = (k - 176) >> 2, t = (k - 176) & 3;
+    const float* b = p + oB2 + 8 * n + 2 * t;
+    o.b2q[n][t] = {b[0], b[1], b[0], b[1]};
+  } else if (k < 192 + 4) {
+    const int t = k - 192;
+    o.w3f[t] = {pair(oW3 + 2 * t), pair(oW3 + 8 + 2 * t), pair(oW3 + 16 + 2 * t),
+                pair(oW3 + 24 + 2 * t)};
+  } else if (k == 196) {
+    o.w3f[4] = {0u, 0u, 0u, 0u};
+  } else if (k == 197) {
+    o.b3 = p[oB3];
+    o.pad[0] = o.pad[1] = o.pad[2] = 0.0f;
   }
-  out->b3 = params[oB3];
+}
+constexpr int kImageWords = 198;
+static_assert(kImageWords * 16 == sizeof(MmaWeights), "one entry per 16-byte word");
+
+inline void build_mma_weights(const float* params, MmaWeights* out) {
+  for (int k = 0; k < kImageWords; ++k) mma_image_entry(params, k, *out, bf16_bits_host);
 }
 
 #if defined(__CUDACC__)
-// all threads of the block: the image at `g` (global memory) into `s`
+// all threads of the block: the image at `g` (global memory) into `s`, 16 bytes per copy
 __device__ __forceinline__ void copy_mma_weights(const MmaWeights* __restrict__ g, MmaWeights& s,
                                                  int tid, int nthreads) {
   const uint4* src = reinterpret_cast<const uint4*>(g);
   uint4* dst = reinterpret_cast<uint4*>(&s);
-  for (int k = tid; k < static_cast<int>(sizeof(MmaWeights) / 16); k += nthreads)
-    dst[k] = __ldg(src + k);
+  for (int k = tid; k < kImageWords; k += nthreads) dst[k] = __ldg(src + k);
 }
 
-// all threads of the block: the image of `w` (kParams floats, weights BF16-valued) into `s`
+// all threads of the block: the image of `w` (kParams floats) into `s`
 __device__ __forceinline__ void stage_mma_weights(const float* __restrict__ w, MmaWeights& s,
                                                   int tid, int nthreads) {
   auto bits = [](float v) {
@@ -148,20 +187,10 @@ __device__ __forceinline__ void stage_mma_weights(const float* __restrict__ w, M
     memcpy(&u, &b, 2);
     return u;
   };
-  uint16_t* w3 = &s.w3[0][0];
-  for (int k = tid; k < 8 * kRowStride; k += nthreads) w3[k] = 0;
-  __syncthreads();
-  for (int k = tid; k < kHid * kIn; k += nthreads) s.w1[k / kIn][k % kIn] = bits(w[oW1 + k]);
-  for (int k = tid; k < kHid * kHid; k += nthreads)
-    s.w2[k / kHid][k % kHid] = bits(w[oW2 + k]);
-  for (int k = tid; k < kHid; k += nthreads) {
-    s.w3[0][k] = bits(w[oW3 + k]);
-    s.b1[k] = w[oB1 + k];
-    s.b2[k] = w[oB2 + k];
-  }
-  if (tid == 0) s.b3 = w[oB3];
+  for (int k = tid; k < kImageWords; k += nthreads) mma_image_entry(w, k, s, bits);
 }
 
+// D += A B, m16n8k16 (BF16 in, FP32 accumulate)
 __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0,
                                          uint32_t b1) {
   asm volatile(
@@ -171,59 +200,106 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-// four 8x8 BF16 matrices; lane L gives the address of row L % 8 of matrix L / 8 and receives
-// in r[j] the elements (row L / 4, columns 2 (L % 4), 2 (L % 4) + 1) of matrix j
-__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void* row) {
-  const unsigned a = static_cast<unsigned>(__cvta_generic_to_shared(row));
-  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-               : "r"(a));
+// D = A B + C, m16n8k16, with C read from a register quad the MMA does not overwrite
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0,
+                                         uint32_t b1, const float4& c) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%10,%11,%12,%13};"
+      : "=f"(d[0]), "=f"(d[1]), "=f"(d[2]), "=f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1), "f"(c.x), "f"(c.y),
+        "f"(c.z), "f"(c.w));
+}
+
+// D = A B + C, m16n8k8 (the 8-input first layer: no zero padding of K)
+__device__ __forceinline__ void mma_bf16_k8(float (&d)[4], const uint32_t (&a)[2], uint32_t b,
+                                            const float4& c) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5}, {%6}, "
+      "{%7,%8,%9,%10};"
+      : "=f"(d[0]), "=f"(d[1]), "=f"(d[2]), "=f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(b), "f"(c.x), "f"(c.y), "f"(c.z), "f"(c.w));
+}
+
+// The 16-byte word kOff bytes past `base` in the image (shared memory).  The offset is an
+// immediate of the load and the load is volatile, so that it stays where it is written: every
+// tile reloads its fragments from three base addresses instead of holding the whole image in
+// registers.
+template <int kOff>
+__device__ __forceinline__ uint4 image_ld(unsigned base) {
+  uint4 r;
+  asm volatile("ld.shared.v4.u32 {%0,%1,%2,%3}, [%4+%5];"
+               : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+               : "r"(base), "n"(kOff));
+  return r;
+}
+
+template <int kOff>
+__device__ __forceinline__ float4 image_ldf(unsigned base) {
+  const uint4 r = image_ld<kOff>(base);
+  return make_float4(__uint_as_float(r.x), __uint_as_float(r.y), __uint_as_float(r.z),
+                     __uint_as_float(r.w));
 }
 
 // The network output for this lane's cell.  All 32 lanes of the warp call it together
-// (converged); xs / ys are the warp's scratch (32 x 4 words, 32 floats) in shared memory.
-// The warp's two 16-row tiles go through the network one after the other (fewer live
-// registers); per tile 4 + 8 + 2 MMAs.  The accumulator fragments of layers 1 and 2, packed to
-// BF16x2 and passed through act2, are the A fragments of layers 2 and 3.
+// (converged); xs / ys are the warp's scratch (32 x 4 words, 32 floats) and w the image, all
+// in shared memory.  The warp's two 16-row tiles go through the network one
+// after the other (fewer live registers); per tile 4 + 8 + 2 MMAs.  The accumulator fragments
+// of layers 1 and 2, packed to BF16x2 and passed through act2, are the A fragments of layers 2
+// and 3; the bias quads are the C operands of each column tile's first MMA.
 __device__ __forceinline__ float forward_warp(const MmaWeights& w, uint4* xs, float* ys,
                                               const float (&xin)[kIn], int lane) {
   xs[lane] = make_uint4(pack_bf16(xin[0], xin[1]), pack_bf16(xin[2], xin[3]),
                         pack_bf16(xin[4], xin[5]), pack_bf16(xin[6], xin[7]));
   __syncwarp();
   const int g = lane >> 2, t = lane & 3;
-  const int lr = lane & 7, lm = lane >> 3;  // ldmatrix: row and matrix this lane addresses
   const uint32_t* xw = reinterpret_cast<const uint32_t*>(xs);
+  const unsigned img = static_cast<unsigned>(__cvta_generic_to_shared(&w));
+  const unsigned lb = img + 16 * lane;               // this lane's fragment words
+  const unsigned tb = img + 16 * t;                  // the bias quads of column pair 2t
+  const unsigned w3b = img + 16 * (g == 0 ? t : 4);  // layer 3: w3 in column 0
+  constexpr int kW1 = offsetof(MmaWeights, w1f), kW2 = offsetof(MmaWeights, w2f);
+  constexpr int kB1 = offsetof(MmaWeights, b1q), kB2 = offsetof(MmaWeights, b2q);
+  constexpr int kW3 = offsetof(MmaWeights, w3f);
 #pragma unroll 1
   for (int m = 0; m < 2; ++m) {
-    const uint32_t a1[4] = {xw[(16 * m + g) * 4 + t], xw[(16 * m + g + 8) * 4 + t], 0u, 0u};
-    uint32_t b1f[4];  // b1f[n]: W1 rows 8n .. 8n + 7
-    ldsm_x4(b1f, &w.w1[lane][0]);
+    // A of layer 1 (m16n8k8): rows g, g + 8 of the tile, inputs 2t, 2t + 1
+    const uint32_t a1[2] = {xw[(16 * m + g) * 4 + t], xw[(16 * m + g + 8) * 4 + t]};
+    const uint4 b1 = image_ld<kW1>(lb);
     uint32_t a2[2][4];
-#pragma unroll
-    for (int n = 0; n < 4; ++n) {
-      const float2 bias = *reinterpret_cast<const float2*>(&w.b1[8 * n + 2 * t]);
-      float d[4] = {bias.x, bias.y, bias.x, bias.y};
-      mma_bf16(d, a1, b1f[n], 0u);
-      a2[n >> 1][(n & 1) * 2] = act2(pack_bf16(d[0], d[1]));
-      a2[n >> 1][(n & 1) * 2 + 1] = act2(pack_bf16(d[2], d[3]));
+    {
+      float d[4];
+      mma_bf16_k8(d, a1, b1.x, image_ldf<kB1 + 0 * 64>(tb));
+      a2[0][0] = act2(pack_bf16(d[0], d[1]));
+      a2[0][1] = act2(pack_bf16(d[2], d[3]));
+      mma_bf16_k8(d, a1, b1.y, image_ldf<kB1 + 1 * 64>(tb));
+      a2[0][2] = act2(pack_bf16(d[0], d[1]));
+      a2[0][3] = act2(pack_bf16(d[2], d[3]));
+      mma_bf16_k8(d, a1, b1.z, image_ldf<kB1 + 2 * 64>(tb));
+      a2[1][0] = act2(pack_bf16(d[0], d[1]));
+      a2[1][1] = act2(pack_bf16(d[2], d[3]));
+      mma_bf16_k8(d, a1, b1.w, image_ldf<kB1 + 3 * 64>(tb));
+      a2[1][2] = act2(pack_bf16(d[0], d[1]));
+      a2[1][3] = act2(pack_bf16(d[2], d[3]));
     }
     uint32_t a3[2][4];
-#pragma unroll
-    for (int n = 0; n < 4; ++n) {
-      uint32_t b[4];  // columns 0-7, 8-15, 16-23, 24-31 of W2 rows 8n .. 8n + 7
-      ldsm_x4(b, &w.w2[8 * n + lr][8 * lm]);
-      const float2 bias = *reinterpret_cast<const float2*>(&w.b2[8 * n + 2 * t]);
-      float d[4] = {bias.x, bias.y, bias.x, bias.y};
-      mma_bf16(d, a2[0], b[0], b[1]);
-      mma_bf16(d, a2[1], b[2], b[3]);
-      a3[n >> 1][(n & 1) * 2] = act2(pack_bf16(d[0], d[1]));
-      a3[n >> 1][(n & 1) * 2 + 1] = act2(pack_bf16(d[2], d[3]));
-    }
-    uint32_t b3f[4];
-    ldsm_x4(b3f, &w.w3[lr][8 * lm]);
-    float d[4] = {0.f, 0.f, 0.f, 0.f};
-    mma_bf16(d, a3[0], b3f[0], b3f[1]);
-    mma_bf16(d, a3[1], b3f[2], b3f[3]);
+    auto layer2 = [&](auto nc, uint32_t& lo0, uint32_t& lo1) {
+      constexpr int n = decltype(nc)::value;
+      const uint4 b = image_ld<kW2 + n * 512>(lb);
+      float d[4];
+      mma_bf16(d, a2[0], b.x, b.y, image_ldf<kB2 + n * 64>(tb));
+      mma_bf16(d, a2[1], b.z, b.w);
+      lo0 = act2(pack_bf16(d[0], d[1]));
+      lo1 = act2(pack_bf16(d[2], d[3]));
+    };
+    layer2(std::integral_constant<int, 0>(), a3[0][0], a3[0][1]);
+    layer2(std::integral_constant<int, 1>(), a3[0][2], a3[0][3]);
+    layer2(std::integral_constant<int, 2>(), a3[1][0], a3[1][1]);
+    layer2(std::integral_constant<int, 3>(), a3[1][2], a3[1][3]);
+    const uint4 b3 = image_ld<kW3>(w3b);
+    float d[4];
+    mma_bf16(d, a3[0], b3.x, b3.y, make_float4(0.f, 0.f, 0.f, 0.f));
+    mma_bf16(d, a3[1], b3.z, b3.w);
     if (t == 0) {  // column 0: rows g and g + 8 of tile m
       ys[16 * m + g] = d[0];
       ys[16 * m + g + 8] = d[2];
