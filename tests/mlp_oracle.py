@@ -1,7 +1,7 @@
 """CPU oracle of the learned closure's network (test infrastructure).
 
 The 8-32-32-1 tanh MLP of tlbm_gb300/csrc/mlp.cuh in FP64 numpy, with the same BF16 roundings
-(weights, inputs, pre-activations and activations) and the same loss, mean of (y - t)^2 / 2.  With
+(weights, inputs and activations) and the same loss, mean of (y - t)^2 / 2.  With
 ``round_bf16=False`` it is the plain FP64 network, used to check its own gradient by finite
 differences.
 """
@@ -49,9 +49,9 @@ def forward_backward(p, X, T, round_bf16=True):
     T = np.asarray(T, np.float64).reshape(-1)
     n = len(T)
     x = r(X)
-    # act(z) = tanh of the BF16-rounded z, delivered in BF16 (mlp.cuh)
-    h1 = r(np.tanh(r(x @ W1.T + b1)))
-    h2 = r(np.tanh(r(h1 @ W2.T + b2)))
+    # act(z) = BF16(tanh(z)) of the FP32 pre-activation (mlp.cuh)
+    h1 = r(np.tanh(x @ W1.T + b1))
+    h2 = r(np.tanh(h1 @ W2.T + b2))
     y = h2 @ w3 + b3
     dy = y - T
     loss = float(np.mean(0.5 * dy * dy))

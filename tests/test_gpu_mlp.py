@@ -203,9 +203,10 @@ def test_fused_tensor_core_closure_matches_oracle():
     rel_w = rate_error(np.maximum(3.0 * (nu + out_scale * y_w) + 0.5, tau_min))
     print("fused closure step: rate error median %.2e, 99th pct %.2e; perturbed network "
           "median %.2e" % (np.median(rel), np.percentile(rel, 99), np.median(rel_w)))
-    # the kernel's activation is the special-function unit's BF16 tanh, which differs from the
-    # oracle's correctly rounded tanh by up to one BF16 ulp (2^-8 relative) per hidden unit:
-    # ~1e-3 in y, ~1e-4 in the rate; FP32 round-off of the populations adds ~1e-5
+    # the kernel's activation rounds the special-function unit's FP32 tanh (relative error below
+    # 2^-10.9) to BF16, which differs from the oracle's BF16 of the exact tanh by one BF16 ulp
+    # (2^-8 relative) where the two straddle a rounding boundary: ~1e-3 in y at most, ~1e-4 in
+    # the rate; FP32 round-off of the populations adds ~1e-5
     assert np.median(rel) <= 5e-4
     assert np.percentile(rel, 99) <= 3e-3
     assert np.median(rel_w) >= 10 * np.median(rel)

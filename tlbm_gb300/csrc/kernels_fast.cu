@@ -39,7 +39,7 @@ constexpr int kMlpMinBlocks = K == kStoreF64 ? 4 : TLBM_MLP_MIN_BLOCKS;
 // collision, which also needs the stress after the network.
 template <class L, int K, bool kReg>
 __device__ __forceinline__ void mlp_cell(const StepArgs& a, const mlp::Closure& cl,
-                                         const mlp::MmaWeights& sw, uint4* xs, float* ys, int x,
+                                         const mlp::MmaWeights& sw, mlp::WarpScratch& ws, int x,
                                          int y, int z, int lane) {
   using S = Store<K>;
   using C = typename S::C;
@@ -81,7 +81,7 @@ __device__ __forceinline__ void mlp_cell(const StepArgs& a, const mlp::Closure& 
   __syncthreads();  // the network is in shared memory
   float net = 0.f;
   if (__any_sync(0xFFFFFFFFu, fluid && relaxes(pb)))
-    net = mlp::forward_warp(sw, xs, ys, xin, lane);
+    net = mlp::forward_warp(sw, ws, xin, lane);
   if (!fluid) return;
   if (relaxes(pb)) {
     launder(ux);
@@ -113,14 +113,13 @@ template <class L, int K, bool kReg>
 __global__ void __launch_bounds__(128, kMlpMinBlocks<K>)
     k_step_fast_mlp(StepArgs a, const mlp::Closure cl) {
   __shared__ mlp::MmaWeights sw;
-  __shared__ uint4 xs[4][32];
-  __shared__ float ys[4][32];
+  __shared__ mlp::WarpScratch ws[4];
   const int tid = threadIdx.x + threadIdx.y * blockDim.x;
   mlp::copy_mma_weights(cl.w, sw, tid, blockDim.x * blockDim.y);
   const int warp = tid >> 5, lane = tid & 31;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  mlp_cell<L, K, kReg>(a, cl, sw, xs[warp], ys[warp], x, y, blockIdx.z, lane);
+  mlp_cell<L, K, kReg>(a, cl, sw, ws[warp], x, y, blockIdx.z, lane);
 }
 
 template <class L, int K>

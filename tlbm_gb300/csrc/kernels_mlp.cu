@@ -192,8 +192,7 @@ __global__ void __launch_bounds__(kTile) k_mlp_predict(const float* __restrict__
                                                        const float* __restrict__ feats, int64_t n,
                                                        float* __restrict__ y) {
   __shared__ MmaWeights sw;
-  __shared__ uint4 xs[kTile / 32][32];
-  __shared__ float ys[kTile / 32][32];
+  __shared__ WarpScratch ws[kTile / 32];
   stage_mma_weights(wbf, sw, threadIdx.x, kTile);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -203,7 +202,7 @@ __global__ void __launch_bounds__(kTile) k_mlp_predict(const float* __restrict__
     float x[kIn];
 #pragma unroll
     for (int k = 0; k < kIn; ++k) x[k] = i < n ? feats[i * kIn + k] : 0.0f;
-    const float v = forward_warp(sw, xs[warp], ys[warp], x, lane);
+    const float v = forward_warp(sw, ws[warp], x, lane);
     if (i < n) y[i] = v;
   }
 }

@@ -9,10 +9,11 @@
 // a non-finite output falls back to the Smagorinsky rate.
 //
 // Weights are BF16 (rounded from FP32 master copies), biases FP32, accumulation FP32.  The
-// activation is act(z) = tanh of z rounded to BF16, evaluated by the special-function unit in
-// BF16 (tanh.approx.bf16, two lanes per instruction in the packed form), so every layer input
-// is a BF16 value.  Training (kernels_mlp.cu) and inference (the fused collide kernel) use the
-// same act, so the network trained is the network run.
+// activation is act(z) = BF16(tanh(z)): the special-function unit's FP32 tanh (tanh.approx.f32,
+// relative error below 2^-10.9) of the FP32 pre-activation, rounded to BF16 once, so every
+// layer input is a BF16 value.  In the tensor-core pass the rounding is the pack of two
+// activations into the BF16x2 word of an A fragment.  Training (kernels_mlp.cu) and inference
+// (the fused collide kernel) use the same act, so the network trained is the network run.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -77,92 +78,123 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
   return u;
 }
 
-// act on two values packed as BF16x2
-__device__ __forceinline__ uint32_t act2(uint32_t zz) {
-  uint32_t r;
-  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(r) : "r"(zz));
+// the special-function unit's tanh of an FP32 value
+__device__ __forceinline__ float tanh_sfu(float z) {
+  float r;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(r) : "f"(z));
   return r;
+}
+
+// act of two FP32 pre-activations, packed as the BF16x2 word (lo in the low half)
+__device__ __forceinline__ uint32_t act2(float lo, float hi) {
+  return pack_bf16(tanh_sfu(lo), tanh_sfu(hi));
 }
 
 // act(z) for one value, as a float holding a BF16 value
 __device__ __forceinline__ float act(float z) {
-  const uint32_t r = act2(pack_bf16(z, 0.0f));
-  return __uint_as_float(r << 16);
+  return __bfloat162float(__float2bfloat16_rn(tanh_sfu(z)));
 }
 #endif
 
 // ---------------------------------------------------------------- tensor-core forward pass
 // Inference inside the collide kernel runs on the tensor cores one warp at a time: the warp's
-// 32 cells form two 16-row tiles, and mma.sync (BF16 in, FP32 accumulate) computes
-//   layer 1: H1[32 x 32] = X[32 x 8] W1^T + b1,  m16n8k8,   8 MMAs
-//   layer 2: H2[32 x 32] = act(H1) W2^T + b2,    m16n8k16, 16 MMAs
-//   layer 3: y[32]       = act(H2) w3 + b3,      m16n8k16,  4 MMAs
-// The FP32 accumulator fragment of layer 1 has the layout of the BF16 A fragment of layer 2
-// (rows g, g+8; columns 2t, 2t+1 of each 8-column tile), so act(H1) is packed to BF16 in
-// registers and fed back without a trip through shared memory; layer 3 (32 -> 1) is one more
-// pair of MMAs with w3 as column 0 of the B tile.
+// 32 cells form two 16-row tiles, and mma.sync m16n8k16 (BF16 in, FP32 accumulate) computes
+//   layer 1: H1[32 x 32] = [X 1 1 1 0..][W1 b1h b1m b1l 0..]^T,   8 MMAs
+//   layer 2: H2[32 x 32] = act(H1) W2^T + b2,                    16 MMAs
+//   layer 3: y[32]       = act(H2) w3 (+ b3 after the exchange),  4 MMAs
+// Layer 1's K runs over the 8 inputs and, in the columns 8..10 the inputs leave free, over
+// three constant ones that multiply the BF16 parts b1h + b1m + b1l = b1 of the FP32 bias (exact:
+// three BF16 significands hold FP32's), so its bias costs no load.  The FP32 accumulator
+// fragment of layer 1 has the layout of the BF16 A fragment of layer 2 (rows g, g+8; columns
+// 2t, 2t+1 of each 8-column tile), so act(H1) is packed to BF16 in registers (two
+// tanh.approx.f32 and one cvt per word) and fed back without a trip through shared memory;
+// layer 3 (32 -> 1) is one more pair of MMAs with w3 as column 0 of the B tile.
 
 // The network as the tensor-core pass reads it: every lane's B fragments, in fragment order,
 // so one 16-byte load hands a lane four fragment registers.  Lane (g, t) = (lane / 4, lane % 4)
 // holds, for column tile n (hidden units 8n .. 8n + 7):
-//   layer 1 (K = 8):  w1f[lane].n    = (W1[8n+g][2t], W1[8n+g][2t+1])
+//   layer 1 (K = 16): w1f[n / 2][lane].(2 (n % 2)) = (W1[8n+g][2t], W1[8n+g][2t+1]),
+//                     w1f[n / 2][lane].(2 (n % 2) + 1) = columns 8 + 2t, 9 + 2t of the bias
+//                     block: (b1h, b1m)[8n+g] for t = 0, (b1l, 0) for t = 1, zero otherwise
 //   layer 2 (K = 32): w2f[n][lane].j = (W2[8n+g][8j+2t], W2[8n+g][8j+2t+1]), j = 0..3
 //                     (j = 0, 1: the k16 step over inputs 0..15; j = 2, 3: inputs 16..31)
 //   layer 3 (N = 1):  w3 is column 0 of the B tile: lanes with g = 0 hold w3f[t] = the pairs
 //                     w3[2t..], w3[8+2t..], w3[16+2t..], w3[24+2t..]; the others the zero row
 //                     w3f[4]
-// and the biases as accumulator quads, bNq[n][t] = (bN[8n+2t], bN[8n+2t+1]) twice: the initial
-// value of the fragment (rows g, g+8; columns 2t, 2t+1) of column tile n, loaded straight into
-// the MMA's C operand.  Matrices W are [output][input]; weights are BF16 bits, biases FP32.
-// Both the collide kernel and the training pass read the image from shared memory.
+// and layer 2's bias as accumulator quads, b2q[n][t] = (b2[8n+2t], b2[8n+2t+1]) twice: the
+// initial value of the fragment (rows g, g+8; columns 2t, 2t+1) of column tile n, loaded
+// straight into the MMA's C operand.  Matrices W are [output][input]; weights are BF16 bits,
+// biases FP32.  Both the collide kernel and the training pass read the image from shared
+// memory.
 struct alignas(16) MmaWeights {
-  uint4 w1f[32];      // [lane]
+  uint4 w1f[2][32];   // [n / 2][lane]
   uint4 w2f[4][32];   // [n][lane]
-  float4 b1q[4][4];   // [n][t]
   float4 b2q[4][4];   // [n][t]
   uint4 w3f[5];       // [t], row 4 = 0
   float b3, pad[3];
 };
 static_assert(sizeof(MmaWeights) % 16 == 0, "copied as 16-byte words");
 
+// A warp's scratch for the forward pass, in shared memory: the 32 cells' layer-1 A rows (the 8
+// inputs, the three constant ones, zeros; BF16, 48-byte rows so that ldmatrix reads the 8 rows
+// of each of its matrices from distinct banks) and the 32 outputs.
+struct alignas(16) WarpScratch {
+  uint4 x[32][3];  // [cell][16-byte column block], block 2 unused
+  float y[32];
+};
+
+// the value of the BF16 bits bits(v), as a float
+template <class Bits>
+__host__ __device__ inline float bf16_value(float v, Bits bits) {
+  const uint32_t u = static_cast<uint32_t>(bits(v)) << 16;
+  float r;
+  memcpy(&r, &u, 4);
+  return r;
+}
+
 // the image from kParams FP32 parameters (weights rounded to BF16 here); bits(v) gives the
 // BF16 bits of v, so host and device build the same image
 template <class Bits>
 __host__ __device__ inline void mma_image_entry(const float* p, int k, MmaWeights& o, Bits bits) {
-  auto pair = [&](int i) {  // p[i], p[i + 1] as one fragment word (p[i] in the low half)
-    return static_cast<uint32_t>(bits(p[i])) | (static_cast<uint32_t>(bits(p[i + 1])) << 16);
+  auto word = [&](float lo, float hi) {  // (lo, hi) as one fragment word (lo in the low half)
+    return static_cast<uint32_t>(bits(lo)) | (static_cast<uint32_t>(bits(hi)) << 16);
   };
+  auto pair = [&](int i) { return word(p[i], p[i + 1]); };
   // k enumerates the 16-byte words of the image
-  if (k < 32) {
-    const int g = k >> 2, t = k & 3;
+  if (k < 64) {
+    const int h = k >> 5, lane = k & 31, g = lane >> 2, t = lane & 3;
     uint32_t r[4];
-    for (int n = 0; n < 4; ++n) r[n] = pair(oW1 + (8 * n + g) * kIn + 2 * t);
-    o.w1f[k] = {r[0], r[1], r[2], r[3]};
-  } else if (k < 32 + 128) {
-    const int n = (k - 32) >> 5, lane = (k - 32) & 31, g = lane >> 2, t = lane & 3;
+    for (int j = 0; j < 2; ++j) {
+      const int n = 2 * h + j;
+      r[2 * j] = pair(oW1 + (8 * n + g) * kIn + 2 * t);
+      // b1 = hi + mid + lo exactly: each part is the BF16 rounding of what is left
+      const float b = p[oB1 + 8 * n + g];
+      const float hi = bf16_value(b, bits), mid = bf16_value(b - hi, bits);
+      const float lo = bf16_value(b - hi - mid, bits);
+      r[2 * j + 1] = t == 0 ? word(hi, mid) : (t == 1 ? word(lo, 0.0f) : 0u);
+    }
+    o.w1f[h][lane] = {r[0], r[1], r[2], r[3]};
+  } else if (k < 64 + 128) {
+    const int n = (k - 64) >> 5, lane = (k - 64) & 31, g = lane >> 2, t = lane & 3;
     uint32_t r[4];
     for (int j = 0; j < 4; ++j) r[j] = pair(oW2 + (8 * n + g) * kHid + 8 * j + 2 * t);
     o.w2f[n][lane] = {r[0], r[1], r[2], r[3]};
-  } else if (k < 160 + 16) {
-    const int n = (k - 160) >> 2, t = (k - 160) & 3;
-    const float* b = p + oB1 + 8 * n + 2 * t;
-    o.b1q[n][t] = {b[0], b[1], b[0], b[1]};
-  } else if (k < 176 + 16) {
-    const int n = (k - 176) >> 2, t = (k - 176) & 3;
+  } else if (k < 192 + 16) {
+    const int n = (k - 192) >> 2, t = (k - 192) & 3;
     const float* b = p + oB2 + 8 * n + 2 * t;
     o.b2q[n][t] = {b[0], b[1], b[0], b[1]};
-  } else if (k < 192 + 4) {
-    const int t = k - 192;
+  } else if (k < 208 + 4) {
+    const int t = k - 208;
     o.w3f[t] = {pair(oW3 + 2 * t), pair(oW3 + 8 + 2 * t), pair(oW3 + 16 + 2 * t),
                 pair(oW3 + 24 + 2 * t)};
-  } else if (k == 196) {
+  } else if (k == 212) {
     o.w3f[4] = {0u, 0u, 0u, 0u};
-  } else if (k == 197) {
+  } else if (k == 213) {
     o.b3 = p[oB3];
     o.pad[0] = o.pad[1] = o.pad[2] = 0.0f;
   }
 }
-constexpr int kImageWords = 198;
+constexpr int kImageWords = 214;
 static_assert(kImageWords * 16 == sizeof(MmaWeights), "one entry per 16-byte word");
 
 inline void build_mma_weights(const float* params, MmaWeights* out) {
@@ -200,6 +232,32 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
+// four 8x8 BF16 matrices; lane L gives the address of row L % 8 of matrix L / 8 and receives
+// in r[j] the elements (row L / 4, columns 2 (L % 4), 2 (L % 4) + 1) of matrix j
+// (row: a shared-memory address)
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], unsigned row) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(row));
+}
+
+// D = A B, m16n8k16 (the zero accumulator is set inside the statement, so no zero registers
+// stay live outside it)
+__device__ __forceinline__ void mma_bf16_z(float (&d)[4], const uint32_t (&a)[4], uint32_t b0,
+                                           uint32_t b1) {
+  asm volatile(
+      "{\n\t"
+      "mov.f32 %0, 0f00000000;\n\t"
+      "mov.f32 %1, 0f00000000;\n\t"
+      "mov.f32 %2, 0f00000000;\n\t"
+      "mov.f32 %3, 0f00000000;\n\t"
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};\n\t"
+      "}"
+      : "=&f"(d[0]), "=&f"(d[1]), "=&f"(d[2]), "=&f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
 // D = A B + C, m16n8k16, with C read from a register quad the MMA does not overwrite
 __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0,
                                          uint32_t b1, const float4& c) {
@@ -209,16 +267,6 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
       : "=f"(d[0]), "=f"(d[1]), "=f"(d[2]), "=f"(d[3])
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1), "f"(c.x), "f"(c.y),
         "f"(c.z), "f"(c.w));
-}
-
-// D = A B + C, m16n8k8 (the 8-input first layer: no zero padding of K)
-__device__ __forceinline__ void mma_bf16_k8(float (&d)[4], const uint32_t (&a)[2], uint32_t b,
-                                            const float4& c) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k8.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5}, {%6}, "
-      "{%7,%8,%9,%10};"
-      : "=f"(d[0]), "=f"(d[1]), "=f"(d[2]), "=f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(b), "f"(c.x), "f"(c.y), "f"(c.z), "f"(c.w));
 }
 
 // The 16-byte word kOff bytes past `base` in the image (shared memory).  The offset is an
@@ -242,71 +290,70 @@ __device__ __forceinline__ float4 image_ldf(unsigned base) {
 }
 
 // The network output for this lane's cell.  All 32 lanes of the warp call it together
-// (converged); xs / ys are the warp's scratch (32 x 4 words, 32 floats) and w the image, all
-// in shared memory.  The warp's two 16-row tiles go through the network one
-// after the other (fewer live registers); per tile 4 + 8 + 2 MMAs.  The accumulator fragments
-// of layers 1 and 2, packed to BF16x2 and passed through act2, are the A fragments of layers 2
-// and 3; the bias quads are the C operands of each column tile's first MMA.
-__device__ __forceinline__ float forward_warp(const MmaWeights& w, uint4* xs, float* ys,
+// (converged); s is the warp's scratch and w the image, both in shared memory.  The warp's two 16-row tiles go through the network one after the other
+// (fewer live registers); per tile 4 + 8 + 2 MMAs.  The accumulator fragments of layers 1 and
+// 2, through act2 (tanh, then the BF16x2 pack), are the A fragments of layers 2 and 3; layer
+// 2's bias quads are the C operands of each column tile's first MMA.
+__device__ __forceinline__ float forward_warp(const MmaWeights& w, WarpScratch& s,
                                               const float (&xin)[kIn], int lane) {
-  xs[lane] = make_uint4(pack_bf16(xin[0], xin[1]), pack_bf16(xin[2], xin[3]),
-                        pack_bf16(xin[4], xin[5]), pack_bf16(xin[6], xin[7]));
+  // this cell's A row: inputs 0..7, then ones in columns 8, 9, 10 (BF16 1.0 = 0x3F80)
+  s.x[lane][0] = make_uint4(pack_bf16(xin[0], xin[1]), pack_bf16(xin[2], xin[3]),
+                            pack_bf16(xin[4], xin[5]), pack_bf16(xin[6], xin[7]));
+  s.x[lane][1] = make_uint4(0x3F803F80u, 0x00003F80u, 0u, 0u);
   __syncwarp();
   const int g = lane >> 2, t = lane & 3;
-  const uint32_t* xw = reinterpret_cast<const uint32_t*>(xs);
+  // ldmatrix rows: matrices 0..3 = (rows 0-7, columns 0-7), (8-15, 0-7), (0-7, 8-15), (8-15, 8-15)
+  const unsigned arow = static_cast<unsigned>(
+      __cvta_generic_to_shared(&s.x[(lane & 7) + ((lane >> 3) & 1) * 8][lane >> 4]));
   const unsigned img = static_cast<unsigned>(__cvta_generic_to_shared(&w));
   const unsigned lb = img + 16 * lane;               // this lane's fragment words
   const unsigned tb = img + 16 * t;                  // the bias quads of column pair 2t
   const unsigned w3b = img + 16 * (g == 0 ? t : 4);  // layer 3: w3 in column 0
   constexpr int kW1 = offsetof(MmaWeights, w1f), kW2 = offsetof(MmaWeights, w2f);
-  constexpr int kB1 = offsetof(MmaWeights, b1q), kB2 = offsetof(MmaWeights, b2q);
-  constexpr int kW3 = offsetof(MmaWeights, w3f);
+  constexpr int kB2 = offsetof(MmaWeights, b2q), kW3 = offsetof(MmaWeights, w3f);
 #pragma unroll 1
   for (int m = 0; m < 2; ++m) {
-    // A of layer 1 (m16n8k8): rows g, g + 8 of the tile, inputs 2t, 2t + 1
-    const uint32_t a1[2] = {xw[(16 * m + g) * 4 + t], xw[(16 * m + g + 8) * 4 + t]};
-    const uint4 b1 = image_ld<kW1>(lb);
+    uint32_t a1[4];  // A of layer 1: rows 16m .. 16m + 15
+    ldsm_x4(a1, arow + 16 * sizeof(s.x[0]) * m);
     uint32_t a2[2][4];
-    {
+    auto layer1 = [&](auto hc) {
+      constexpr int h = decltype(hc)::value;  // column tiles 2h, 2h + 1
+      const uint4 b = image_ld<kW1 + h * 512>(lb);
       float d[4];
-      mma_bf16_k8(d, a1, b1.x, image_ldf<kB1 + 0 * 64>(tb));
-      a2[0][0] = act2(pack_bf16(d[0], d[1]));
-      a2[0][1] = act2(pack_bf16(d[2], d[3]));
-      mma_bf16_k8(d, a1, b1.y, image_ldf<kB1 + 1 * 64>(tb));
-      a2[0][2] = act2(pack_bf16(d[0], d[1]));
-      a2[0][3] = act2(pack_bf16(d[2], d[3]));
-      mma_bf16_k8(d, a1, b1.z, image_ldf<kB1 + 2 * 64>(tb));
-      a2[1][0] = act2(pack_bf16(d[0], d[1]));
-      a2[1][1] = act2(pack_bf16(d[2], d[3]));
-      mma_bf16_k8(d, a1, b1.w, image_ldf<kB1 + 3 * 64>(tb));
-      a2[1][2] = act2(pack_bf16(d[0], d[1]));
-      a2[1][3] = act2(pack_bf16(d[2], d[3]));
-    }
+      mma_bf16_z(d, a1, b.x, b.y);
+      a2[h][0] = act2(d[0], d[1]);
+      a2[h][1] = act2(d[2], d[3]);
+      mma_bf16_z(d, a1, b.z, b.w);
+      a2[h][2] = act2(d[0], d[1]);
+      a2[h][3] = act2(d[2], d[3]);
+    };
+    layer1(std::integral_constant<int, 0>());
+    layer1(std::integral_constant<int, 1>());
     uint32_t a3[2][4];
-    auto layer2 = [&](auto nc, uint32_t& lo0, uint32_t& lo1) {
+    auto layer2 = [&](auto nc) {
       constexpr int n = decltype(nc)::value;
       const uint4 b = image_ld<kW2 + n * 512>(lb);
       float d[4];
       mma_bf16(d, a2[0], b.x, b.y, image_ldf<kB2 + n * 64>(tb));
       mma_bf16(d, a2[1], b.z, b.w);
-      lo0 = act2(pack_bf16(d[0], d[1]));
-      lo1 = act2(pack_bf16(d[2], d[3]));
+      a3[n >> 1][(n & 1) * 2] = act2(d[0], d[1]);
+      a3[n >> 1][(n & 1) * 2 + 1] = act2(d[2], d[3]);
     };
-    layer2(std::integral_constant<int, 0>(), a3[0][0], a3[0][1]);
-    layer2(std::integral_constant<int, 1>(), a3[0][2], a3[0][3]);
-    layer2(std::integral_constant<int, 2>(), a3[1][0], a3[1][1]);
-    layer2(std::integral_constant<int, 3>(), a3[1][2], a3[1][3]);
+    layer2(std::integral_constant<int, 0>());
+    layer2(std::integral_constant<int, 1>());
+    layer2(std::integral_constant<int, 2>());
+    layer2(std::integral_constant<int, 3>());
     const uint4 b3 = image_ld<kW3>(w3b);
-    float d[4];
-    mma_bf16(d, a3[0], b3.x, b3.y, make_float4(0.f, 0.f, 0.f, 0.f));
-    mma_bf16(d, a3[1], b3.z, b3.w);
+    float y[4];
+    mma_bf16_z(y, a3[0], b3.x, b3.y);
+    mma_bf16(y, a3[1], b3.z, b3.w);
     if (t == 0) {  // column 0: rows g and g + 8 of tile m
-      ys[16 * m + g] = d[0];
-      ys[16 * m + g + 8] = d[2];
+      s.y[16 * m + g] = y[0];
+      s.y[16 * m + g + 8] = y[2];
     }
   }
   __syncwarp();
-  const float y = ys[lane] + w.b3;
+  const float y = s.y[lane] + w.b3;
   __syncwarp();  // the scratch may be reused by the next call
   return y;
 }
