@@ -290,10 +290,13 @@ __device__ __forceinline__ float4 image_ldf(unsigned base) {
 }
 
 // The network output for this lane's cell.  All 32 lanes of the warp call it together
-// (converged); s is the warp's scratch and w the image, both in shared memory.  The warp's two 16-row tiles go through the network one after the other
-// (fewer live registers); per tile 4 + 8 + 2 MMAs.  The accumulator fragments of layers 1 and
-// 2, through act2 (tanh, then the BF16x2 pack), are the A fragments of layers 2 and 3; layer
-// 2's bias quads are the C operands of each column tile's first MMA.
+// (converged); s is the warp's scratch and w the image, both in shared memory.  The warp's two
+// 16-row tiles go through the network one after the other (fewer live registers); per tile
+// 4 + 8 + 2 MMAs.  The accumulator fragments of layers 1 and 2, through act2 (tanh, then the
+// BF16x2 pack), are the A fragments of layers 2 and 3; layer 2's bias quads are the C operands
+// of each column tile's first MMA.  Fragment loads are volatile with immediate offsets
+// (image_ld), and the zero accumulators are set inside the MMA statements, so the image and
+// the constants stay out of the registers between uses.
 __device__ __forceinline__ float forward_warp(const MmaWeights& w, WarpScratch& s,
                                               const float (&xin)[kIn], int lane) {
   // this cell's A row: inputs 0..7, then ones in columns 8, 9, 10 (BF16 1.0 = 0x3F80)
