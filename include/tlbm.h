@@ -291,7 +291,9 @@ tlbm_status tlbm_ensemble_create(int n, const tlbm_problem* problems,
                                  const int32_t* const* nd_types, const tlbm_options* opt,
                                  tlbm_ensemble** out);
 tlbm_status tlbm_ensemble_destroy(tlbm_ensemble* e);
-/* Tile shape: block_x threads (multiple of 32) x block_y rows, cells_per_thread along x. */
+/* Tile shape: block_x * block_y threads (block_x a multiple of 32, at most 256 threads), each
+ * taking cells_per_thread cells; a tile is that many consecutive cells of one z-plane of one
+ * channel, in x-fastest order, so its shape does not depend on the channel's width. */
 tlbm_status tlbm_ensemble_set_tiles(tlbm_ensemble* e, int block_x, int block_y,
                                     int cells_per_thread);
 /* Times each candidate tile shape over `steps` steps, keeps the fastest, then returns every

@@ -81,7 +81,7 @@ Status Ensemble::init(int n, const tlbm_problem* probs, const int32_t* const* nd
     if (p.nx < 1 || p.ny < 1 || p.nz < 1 || p.nz > 65535)
       return Status::err(TLBM_ERR_INVALID_ARGUMENT, "channel " + std::to_string(k) + ": bad size");
     const int64_t cells = static_cast<int64_t>(p.nx) * p.ny * p.nz;
-    if (cells >= (int64_t(1) << 31))
+    if (cells >= (int64_t(1) << 31) || static_cast<int64_t>(p.nx) * p.ny * 8 >= (int64_t(1) << 31))
       return Status::err(TLBM_ERR_UNSUPPORTED, "channel too large");
     for (int64_t g = 0; g < cells; ++g) {
       const int32_t t = nd_types[k][g];
@@ -107,6 +107,7 @@ Status Ensemble::init(int n, const tlbm_problem* probs, const int32_t* const* nd
     pb.dynamics = p.dynamics;
     pb.has_type5 = 0;
     fill_derived(pb, q, sb_);
+    c.div_nx = make_fast_div(static_cast<uint32_t>(p.nx));
     off_type[k] = total;
     total += align(static_cast<size_t>(cells));
     off_f[k] = total;
@@ -138,7 +139,7 @@ Status Ensemble::init(int n, const tlbm_problem* probs, const int32_t* const* nd
   TLBM_CUDA(cudaMalloc(&d_partial_, max_nb * sizeof(double)));
   TLBM_CUDA(cudaMalloc(&d_mass_, sizeof(double)));
   TLBM_TRY(reset_populations());
-  return set_tiles(opt_.block_x > 0 ? opt_.block_x : 32, opt_.block_y > 0 ? opt_.block_y : 4, 1);
+  return set_tiles(opt_.block_x > 0 ? opt_.block_x : 128, opt_.block_y > 0 ? opt_.block_y : 1, 1);
 }
 
 Status Ensemble::reset_populations() {
@@ -161,19 +162,20 @@ Status Ensemble::set_tiles(int bx, int by, int cpt) {
     return Status::err(TLBM_ERR_INVALID_ARGUMENT,
                        "tiles: bx a multiple of 32, bx*by <= 256, 1 <= cells_per_thread <= 8");
   TLBM_CUDA(cudaStreamSynchronize(stream_));
-  std::vector<uint16_t> tiles;
-  int begin = 0;
+  // a tile: bx*by threads x cpt consecutive cells of one z-plane
+  const int cells = bx * by * cpt;
+  std::vector<EnsembleTile> tiles;
   for (size_t k = 0; k < ch_.size(); ++k) {
-    EnsembleChannel& c = ch_[k];
-    c.tiles_x = (c.pb().nx + bx * cpt - 1) / (bx * cpt);
-    c.tiles_y = (c.pb().ny + by - 1) / by;
-    c.tile_begin = begin;
-    const int64_t nt = static_cast<int64_t>(c.tiles_x) * c.tiles_y * c.pb().nz;
-    if (begin + nt > (int64_t(1) << 30)) return Status::err(TLBM_ERR_UNSUPPORTED, "too many tiles");
-    tiles.insert(tiles.end(), static_cast<size_t>(nt), static_cast<uint16_t>(k));
-    begin += static_cast<int>(nt);
+    const EnsembleChannel& c = ch_[k];
+    const int per_plane = (c.pb().nxy + cells - 1) / cells;
+    if (static_cast<int64_t>(tiles.size()) + static_cast<int64_t>(per_plane) * c.pb().nz >
+        (int64_t(1) << 30))
+      return Status::err(TLBM_ERR_UNSUPPORTED, "too many tiles");
+    for (int z = 0; z < c.pb().nz; ++z)
+      for (int t = 0; t < per_plane; ++t)
+        tiles.push_back({static_cast<int>(k), z, t * cells, 0});
   }
-  n_tiles_ = begin;
+  n_tiles_ = static_cast<int>(tiles.size());
   cudaFree(d_ch_);
   cudaFree(d_tiles_);
   d_ch_ = nullptr;
@@ -181,8 +183,8 @@ Status Ensemble::set_tiles(int bx, int by, int cpt) {
   TLBM_CUDA(cudaMalloc(&d_ch_, ch_.size() * sizeof(EnsembleChannel)));
   TLBM_CUDA(cudaMemcpy(d_ch_, ch_.data(), ch_.size() * sizeof(EnsembleChannel),
                        cudaMemcpyHostToDevice));
-  TLBM_CUDA(cudaMalloc(&d_tiles_, tiles.size() * sizeof(uint16_t)));
-  TLBM_CUDA(cudaMemcpy(d_tiles_, tiles.data(), tiles.size() * sizeof(uint16_t),
+  TLBM_CUDA(cudaMalloc(&d_tiles_, tiles.size() * sizeof(EnsembleTile)));
+  TLBM_CUDA(cudaMemcpy(d_tiles_, tiles.data(), tiles.size() * sizeof(EnsembleTile),
                        cudaMemcpyHostToDevice));
   int sms = 0;
   TLBM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, opt_.device));
@@ -198,13 +200,11 @@ Status Ensemble::set_tiles(int bx, int by, int cpt) {
 Status Ensemble::enqueue(int is_even) {
   EnsembleArgs a{};
   a.channels = d_ch_;
-  a.tile_channel = d_tiles_;
+  a.tiles = d_tiles_;
   a.n_tiles = n_tiles_;
   a.src = is_even ? 0 : 1;
-  a.bx = bx_;
-  a.by = by_;
   a.cells_per_thread = cpt_;
-  TLBM_CUDA(launch_ensemble_step(store_, a, grid_, stream_));
+  TLBM_CUDA(launch_ensemble_step(store_, a, bx_ * by_, grid_, stream_));
   ++launches_;
   last_src_ = a.src;
   return Status::ok();
@@ -260,10 +260,10 @@ Status Ensemble::time_steps(int first_ts, int nsteps, float* ms) {
   return s;
 }
 
-// Tile shapes tried by the autotuner: (threads along x, rows, cells per thread along x).
-static const int kCandidates[][3] = {{32, 4, 1}, {32, 8, 1}, {64, 2, 1}, {64, 4, 1},
-                                     {128, 1, 1}, {128, 2, 1}, {32, 4, 2}, {32, 2, 2},
-                                     {64, 2, 2}, {32, 8, 2}};
+// Tile shapes tried by the autotuner: (threads, 1, cells per thread); a tile is threads x cells
+// per thread consecutive cells of a z-plane.
+static const int kCandidates[][3] = {{64, 1, 1},  {128, 1, 1}, {256, 1, 1}, {64, 1, 2},
+                                     {128, 1, 2}, {256, 1, 2}, {128, 1, 4}, {256, 1, 4}};
 
 Status Ensemble::autotune(int steps, int* bx, int* by, int* cpt) {
   if (steps < 2) steps = 2;

@@ -63,14 +63,36 @@ __device__ __forceinline__ void node_macros(uint8_t t, const C (&f)[L::Q], C u_b
   }
 }
 
-// the Q stored values cell c pulls (from c - e_i, periodic)
-template <class L, int K>
+// the Q stored values cell c pulls (from c - e_i, periodic).  kWrapFree: cells on the x and y
+// edges of a plane take the interior path too, their wrap folded into the offsets by selects
+// (no divergent second path in a warp that spans a whole row of a narrow lattice); z-edge
+// planes, uniform across a warp, keep the neighbour-table path.  Same values either way.
+template <class L, int K, bool kWrapFree = false>
 __device__ __forceinline__ void load_raw(const StepArgs& a, int x, int y, int z, int c,
                                          typename Store<K>::T (&raw)[L::Q]) {
   using S = Store<K>;
   using P = typename S::P;
   const DevProblem& pb = a.pb;
   const P* __restrict__ src = static_cast<const P*>(a.src);
+  if constexpr (kWrapFree && !S::kMoment) {
+    if (z > 0 && z < pb.nz - 1) {
+      // speed i pulls from x - ex_i: from the far edge when that leaves the plane
+      constexpr int b = static_cast<int>(sizeof(P));
+      const int wx_pos = x == 0 ? pb.nx * b : 0;               // ex > 0 at x = 0
+      const int wx_neg = x == pb.nx - 1 ? -pb.nx * b : 0;      // ex < 0 at x = nx - 1
+      const int wy_pos = y == 0 ? pb.nxy * b : 0;              // ey > 0 at y = 0
+      const int wy_neg = y == pb.ny - 1 ? -pb.nxy * b : 0;     // ey < 0 at y = ny - 1
+      const char* base = reinterpret_cast<const char*>(src + c);
+#pragma unroll
+      for (int i = 0; i < L::Q; ++i) {
+        const int ex = L::ex(i), ey = L::ey(i);
+        const int w = (ex > 0 ? wx_pos : (ex < 0 ? wx_neg : 0)) +
+                      (ey > 0 ? wy_pos : (ey < 0 ? wy_neg : 0));
+        raw[i] = __ldg(reinterpret_cast<const P*>(base + pb.pull_off[i] + w));
+      }
+      return;
+    }
+  }
   if (x > 0 && x < pb.nx - 1 && y > 0 && y < pb.ny - 1 && z > 0 && z < pb.nz - 1) {
     // interior cell: speed i comes from a fixed byte offset of the cell's own slot
     const char* base = reinterpret_cast<const char*>(src + c);
@@ -194,15 +216,16 @@ __device__ __forceinline__ void accumulate_avg(const StepArgs& a, int c, C rho, 
 }
 
 // kClosure: fast::kClosureNone (BGK) or kClosureSmag (the learned closure has its own kernel,
-// kernels_fast.cu: k_step_fast_mlp); kReg: the moment-space collision (RBGK / MRT)
-template <class L, int K, int kClosure, bool kReg = false>
+// kernels_fast.cu: k_step_fast_mlp); kReg: the moment-space collision (RBGK / MRT);
+// kWrapFree: load_raw's branch-free x/y wrap
+template <class L, int K, int kClosure, bool kReg = false, bool kWrapFree = false>
 __device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z) {
   using S = Store<K>;
   using C = typename S::C;
   const DevProblem& pb = a.pb;
   const int c = x + y * pb.nx + z * pb.nxy;
   typename S::T raw[L::Q];
-  load_raw<L, K>(a, x, y, z, c, raw);
+  load_raw<L, K, kWrapFree>(a, x, y, z, c, raw);
   const uint8_t t = pb.nd_type[c];
   C rho = 0, ux = 0, uy = 0, uz = 0;
   if (t == kFluid) {
