@@ -81,7 +81,7 @@ Status Ensemble::init(int n, const tlbm_problem* probs, const int32_t* const* nd
     if (p.nx < 1 || p.ny < 1 || p.nz < 1 || p.nz > 65535)
       return Status::err(TLBM_ERR_INVALID_ARGUMENT, "channel " + std::to_string(k) + ": bad size");
     const int64_t cells = static_cast<int64_t>(p.nx) * p.ny * p.nz;
-    if (cells >= (int64_t(1) << 31) || static_cast<int64_t>(p.nx) * p.ny * 8 >= (int64_t(1) << 31))
+    if (cells >= (int64_t(1) << 31))
       return Status::err(TLBM_ERR_UNSUPPORTED, "channel too large");
     for (int64_t g = 0; g < cells; ++g) {
       const int32_t t = nd_types[k][g];

@@ -65,9 +65,10 @@ __device__ __forceinline__ void node_macros(uint8_t t, const C (&f)[L::Q], C u_b
 
 // the Q stored values cell c pulls (from c - e_i, periodic).  kWrapFree: cells on the x and y
 // edges of a plane take the interior path too, their wrap folded into the offsets by selects
-// (no divergent second path in a warp that spans a whole row of a narrow lattice); z-edge
-// planes, uniform across a warp, keep the neighbour-table path.  Same values either way.
-template <class L, int K, bool kWrapFree = false>
+// (no divergent second path in the warps that hold an x edge: every warp of a narrow lattice);
+// z-edge planes, uniform across a warp, and planes whose byte size does not fit the 32-bit
+// offsets keep the neighbour-table path.  Same values either way.
+template <class L, int K, bool kWrapFree = true>
 __device__ __forceinline__ void load_raw(const StepArgs& a, int x, int y, int z, int c,
                                          typename Store<K>::T (&raw)[L::Q]) {
   using S = Store<K>;
@@ -75,7 +76,8 @@ __device__ __forceinline__ void load_raw(const StepArgs& a, int x, int y, int z,
   const DevProblem& pb = a.pb;
   const P* __restrict__ src = static_cast<const P*>(a.src);
   if constexpr (kWrapFree && !S::kMoment) {
-    if (z > 0 && z < pb.nz - 1) {
+    constexpr int kMaxPlane = 0x7FFFFFFF / static_cast<int>(sizeof(P));
+    if (z > 0 && z < pb.nz - 1 && pb.nxy <= kMaxPlane - pb.nx) {  // |wx + wy| fits an int
       // speed i pulls from x - ex_i: from the far edge when that leaves the plane
       constexpr int b = static_cast<int>(sizeof(P));
       const int wx_pos = x == 0 ? pb.nx * b : 0;               // ex > 0 at x = 0
@@ -218,7 +220,7 @@ __device__ __forceinline__ void accumulate_avg(const StepArgs& a, int c, C rho, 
 // kClosure: fast::kClosureNone (BGK) or kClosureSmag (the learned closure has its own kernel,
 // kernels_fast.cu: k_step_fast_mlp); kReg: the moment-space collision (RBGK / MRT);
 // kWrapFree: load_raw's branch-free x/y wrap
-template <class L, int K, int kClosure, bool kReg = false, bool kWrapFree = false>
+template <class L, int K, int kClosure, bool kReg = false, bool kWrapFree = true>
 __device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z) {
   using S = Store<K>;
   using C = typename S::C;
