@@ -452,6 +452,8 @@ class Ensemble:
             raise TLBMError(st, self._L.tlbm_ensemble_last_error(self._h).decode())
 
     def set_tiles(self, bx, by, cells_per_thread=1):
+        """bx * by threads per block (bx a multiple of 32, at most 256), each taking
+        cells_per_thread cells: a tile is that many consecutive cells of one z-plane."""
         self._check(self._L.tlbm_ensemble_set_tiles(self._h, bx, by, cells_per_thread))
 
     def autotune(self, steps=20):
