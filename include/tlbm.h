@@ -181,6 +181,22 @@ tlbm_status tlbm_copy_macros(tlbm_handle* h, void* ux, void* uy, void* uz, void*
 /* Force of calc_force (src/TLBM_Partition.cpp:174-208) on the last step, global order. */
 tlbm_status tlbm_copy_force(tlbm_handle* h, void* fx, void* fy, void* fz);
 
+/* The seven write_data fields (ux, uy, uz, rho, Fx, Fy, Fz; any pointer may be NULL) of the last
+ * step, as tlbm_copy_macros + tlbm_copy_force, but the call returns once the device-to-host
+ * copies are queued on the handle's copy stream: the next time steps run while they proceed.
+ * The host buffers (page-locked ones from tlbm_host_alloc; pageable memory makes the copies
+ * synchronous) hold the values after tlbm_synchronize(h); they must not be read or freed
+ * before.  A later output computation waits for these copies. */
+tlbm_status tlbm_copy_outputs_async(tlbm_handle* h, void* ux, void* uy, void* uz, void* rho,
+                                    void* fx, void* fy, void* fz);
+
+/* Page-locked host memory for the tlbm_copy_* destinations (no counterpart in the reference,
+ * whose write_data goes through its own buffers): copies into it run at the host link's rate
+ * (~190 GB/s on GB300 against 13-25 GB/s into fresh pageable memory).  A failure leaves *out
+ * NULL, with the message in tlbm_get_last_error(NULL).  tlbm_host_free(NULL) is a no-op. */
+tlbm_status tlbm_host_alloc(size_t bytes, void** out);
+tlbm_status tlbm_host_free(void* p);
+
 /* Populations in the reference's layout f[node*Q + speed] (getIDx, include/TLBM_Partition.h:57):
  * which = 0: after streaming (the reference's fOut); which = 1: after collision, before
  * streaming (the reference's fIn at the end of a step). */

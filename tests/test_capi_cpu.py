@@ -205,3 +205,13 @@ def test_option_combinations_refused_before_the_device(lib, kw, dynamics, status
     nd = np.zeros(8 * 8 * 12, np.int32)
     st, msg = _create(_problem(8, 8, 12, dynamics), nd, **kw)
     assert st == status and msg
+
+
+def test_host_alloc_arguments(lib):
+    """tlbm_host_alloc refuses a NULL out-pointer and a zero size before calling CUDA;
+    tlbm_host_free(NULL) is a no-op."""
+    assert lib.tlbm_host_alloc(16, None) == T.ERR_INVALID_ARGUMENT
+    p = ctypes.c_void_p(1)
+    assert lib.tlbm_host_alloc(0, ctypes.byref(p)) == T.ERR_INVALID_ARGUMENT
+    assert p.value is None
+    assert lib.tlbm_host_free(None) == T.OK

@@ -317,3 +317,54 @@ def test_bf16m_restart_and_steps_close_to_f32(q):
         e_m = np.abs(np.asarray(out["bf16m"][1][k], np.float64) - ref)
         e_b = np.abs(np.asarray(out["bf16"][1][k], np.float64) - ref)
         assert e_m.max() <= 5e-4 and rms(e_m) < rms(e_b), k
+
+
+def test_copies_into_page_locked_host_buffers():
+    """macros(out=...) / force(out=...) into host_empty (tlbm_host_alloc) buffers: the same
+    values as fresh arrays, in the buffers given; malformed destinations are refused."""
+    g = G.sphere_in_box(12, 10, 24, 3, 6, 5, 8)
+    p = G.params_lattice_units(g, "D3Q19", 0.04, 30.0, 6.0, 12, cs=0.1)
+    part = T.TLBMPartition.from_arrays(T.problem_from_params(p), g.nd_type, precision="f32",
+                                       arithmetic="fast")
+    part.run(0, 7)
+    want = part.macros() + part.force()
+    host = [T.host_empty(part.n, np.float32) for _ in range(7)]
+    got = part.macros(out=host[:4]) + part.force(out=host[4:])
+    assert all(a is b for a, b in zip(got, host))
+    for a, b in zip(got, want):
+        assert np.array_equal(a, b)
+    with pytest.raises(ValueError):
+        part.macros(out=[np.empty(part.n, np.float64)] * 4)
+    with pytest.raises(ValueError):
+        part.force(out=host[:2])
+    part.close()
+    del host, got
+
+
+def test_async_output_copies_overlap_later_steps():
+    """tlbm_copy_outputs_async: the values of the step it was called after, although more steps
+    run before the copies are waited for; a second call recomputes after the first copies."""
+    g = G.sphere_in_box(12, 10, 24, 3, 6, 5, 8)
+    p = G.params_lattice_units(g, "D3Q19", 0.04, 30.0, 6.0, 12, cs=0.1)
+    a = T.TLBMPartition.from_arrays(T.problem_from_params(p), g.nd_type, precision="f64",
+                                    arithmetic="fast")
+    b = T.TLBMPartition.from_arrays(T.problem_from_params(p), g.nd_type, precision="f64",
+                                    arithmetic="fast")
+    a.run(0, 5)
+    b.run(0, 5)
+    want5 = b.macros() + b.force()
+    b.run(5, 4)
+    want9 = b.macros() + b.force()
+    h5 = [T.host_empty(a.n, np.float64) for _ in range(7)]
+    h9 = [T.host_empty(a.n, np.float64) for _ in range(7)]
+    a.outputs_async(h5)
+    a.run(5, 4)
+    a.outputs_async(h9)
+    a.run(9, 3)
+    a.synchronize()
+    for x, y in zip(h5, want5):
+        assert np.array_equal(x, y)
+    for x, y in zip(h9, want9):
+        assert np.array_equal(x, y)
+    a.close()
+    b.close()

@@ -19,6 +19,7 @@ from __future__ import annotations
 import ctypes
 import os
 import re
+import weakref
 
 import numpy as np
 
@@ -104,6 +105,9 @@ def library(path: str = LIB_PATH):
         "tlbm_num_speeds": (i32, [H]),
         "tlbm_copy_macros": (i32, [H, vp, vp, vp, vp]),
         "tlbm_copy_force": (i32, [H, vp, vp, vp]),
+        "tlbm_copy_outputs_async": (i32, [H, vp, vp, vp, vp, vp, vp, vp]),
+        "tlbm_host_alloc": (i32, [ctypes.c_size_t, PH]),
+        "tlbm_host_free": (i32, [vp]),
         "tlbm_copy_populations": (i32, [H, i32, vp]),
         "tlbm_copy_adjacency": (i32, [H, vp]),
         "tlbm_mass": (i32, [H, ctypes.POINTER(ctypes.c_double)]),
@@ -131,6 +135,22 @@ def library(path: str = LIB_PATH):
         fn.argtypes = args
     _lib = L
     return L
+
+
+def host_empty(n: int, dtype) -> np.ndarray:
+    """An uninitialised array of n values in page-locked host memory (tlbm_host_alloc): the
+    destination of choice for macros(out=...) and force(out=...), whose copies then run at the
+    host link's rate.  The memory is released when the array is garbage-collected."""
+    L = library()
+    dtype = np.dtype(dtype)
+    nbytes = max(1, int(n) * dtype.itemsize)
+    ptr = ctypes.c_void_p()
+    st = L.tlbm_host_alloc(nbytes, ctypes.byref(ptr))
+    if st != OK:
+        raise TLBMError(st, L.tlbm_get_last_error(None).decode())
+    buf = (ctypes.c_char * nbytes).from_address(ptr.value)
+    weakref.finalize(buf, L.tlbm_host_free, ctypes.c_void_p(ptr.value))
+    return np.frombuffer(buf, dtype=dtype, count=int(n))
 
 
 def process_output_dir(workdir: str, device: int = 0) -> int:
@@ -271,14 +291,35 @@ class TLBMPartition:
     def synchronize(self) -> None:
         _check(self._L.tlbm_synchronize(self._h), self._h)
 
-    def macros(self):
-        out = [np.empty(self.n, self.dtype) for _ in range(4)]
+    def _outputs(self, k, out):
+        if out is None:
+            return [np.empty(self.n, self.dtype) for _ in range(k)]
+        out = list(out)
+        if len(out) != k or any(a.dtype != self.dtype or a.size != self.n or
+                                not a.flags.c_contiguous or not a.flags.writeable for a in out):
+            raise ValueError("out: %d writeable contiguous %s arrays of %d values"
+                             % (k, np.dtype(self.dtype).name, self.n))
+        return out
+
+    def macros(self, out=None):
+        """ux, uy, uz, rho of the last step (global order); out: 4 arrays to fill, e.g. from
+        host_empty (page-locked), instead of new ones."""
+        out = self._outputs(4, out)
         _check(self._L.tlbm_copy_macros(self._h, *[a.ctypes.data for a in out]), self._h)
         return out
 
-    def force(self):
-        out = [np.empty(self.n, self.dtype) for _ in range(3)]
+    def force(self, out=None):
+        """Fx, Fy, Fz of the last step (global order); out as for macros."""
+        out = self._outputs(3, out)
         _check(self._L.tlbm_copy_force(self._h, *[a.ctypes.data for a in out]), self._h)
+        return out
+
+    def outputs_async(self, out):
+        """Start copying ux, uy, uz, rho, Fx, Fy, Fz of the last step into the 7 arrays `out`
+        (page-locked: host_empty) while later steps run (tlbm_copy_outputs_async); they hold
+        the values after synchronize()."""
+        out = self._outputs(7, out)
+        _check(self._L.tlbm_copy_outputs_async(self._h, *[a.ctypes.data for a in out]), self._h)
         return out
 
     def populations(self, which: int = 0):

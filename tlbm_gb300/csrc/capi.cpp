@@ -221,6 +221,32 @@ tlbm_status tlbm_copy_macros(tlbm_handle* h, void* ux, void* uy, void* uz, void*
 tlbm_status tlbm_copy_force(tlbm_handle* h, void* fx, void* fy, void* fz) {
   TLBM_CALL(h, h->engine->copy_force(fx, fy, fz));
 }
+tlbm_status tlbm_copy_outputs_async(tlbm_handle* h, void* ux, void* uy, void* uz, void* rho,
+                                    void* fx, void* fy, void* fz) {
+  void* const host[7] = {ux, uy, uz, rho, fx, fy, fz};
+  TLBM_CALL(h, h->engine->copy_outputs_async(host));
+}
+tlbm_status tlbm_host_alloc(size_t bytes, void** out) {
+  if (!out) return TLBM_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (bytes == 0) return fail_create(tlbm::Status::err(TLBM_ERR_INVALID_ARGUMENT, "0 bytes"));
+  const cudaError_t e = cudaMallocHost(out, bytes);
+  if (e != cudaSuccess) {
+    *out = nullptr;
+    return fail_create(tlbm::Status::err(e == cudaErrorMemoryAllocation ? TLBM_ERR_NO_MEMORY
+                                                                        : TLBM_ERR_CUDA,
+                                         std::string("cudaMallocHost: ") + cudaGetErrorString(e)));
+  }
+  return TLBM_OK;
+}
+tlbm_status tlbm_host_free(void* p) {
+  if (!p) return TLBM_OK;
+  const cudaError_t e = cudaFreeHost(p);
+  if (e != cudaSuccess)
+    return fail_create(tlbm::Status::err(TLBM_ERR_CUDA,
+                                         std::string("cudaFreeHost: ") + cudaGetErrorString(e)));
+  return TLBM_OK;
+}
 tlbm_status tlbm_copy_populations(tlbm_handle* h, int which, void* out) {
   if (!out) return TLBM_ERR_INVALID_ARGUMENT;
   TLBM_CALL(h, h->engine->copy_populations(which, out));

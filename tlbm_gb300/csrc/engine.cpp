@@ -228,6 +228,7 @@ Status Engine::check(cudaError_t e, const char* what) {
 
 Engine::~Engine() {
   if (stream_) cudaStreamSynchronize(stream_);
+  if (copy_stream_) cudaStreamSynchronize(copy_stream_);
   for (auto& g : graph_)
     if (g) cudaGraphExecDestroy(g);
   cudaFree(d_type_);
@@ -247,6 +248,9 @@ Engine::~Engine() {
   cudaFree(d_ss_);
   cudaFree(d_ss_stage_);
   if (h_pinned_) cudaFreeHost(h_pinned_);
+  if (outputs_ready_) cudaEventDestroy(outputs_ready_);
+  if (copies_done_) cudaEventDestroy(copies_done_);
+  if (copy_stream_) cudaStreamDestroy(copy_stream_);
   if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -634,6 +638,8 @@ Status Engine::time_steps(int first_ts, int nsteps, float* ms) {
 Status Engine::synchronize() {
   TLBM_CUDA(cudaSetDevice(opt_.device));
   TLBM_CUDA(cudaStreamSynchronize(stream_));
+  if (copy_stream_) TLBM_CUDA(cudaStreamSynchronize(copy_stream_));
+  copies_pending_ = false;
   return Status::ok();
 }
 
@@ -641,6 +647,8 @@ Status Engine::compute_outputs() {
   if (last_src_ < 0)
     return Status::err(TLBM_ERR_INVALID_ARGUMENT, "no time step has been taken yet");
   if (outputs_fresh_) return Status::ok();
+  // an asynchronous copy may still be reading the output fields
+  if (copies_pending_) TLBM_CUDA(cudaStreamWaitEvent(stream_, copies_done_, 0));
   // macroscopic values of the last step, recomputed from its (untouched) pull source
   if (ref_arith_) {
     TLBM_CUDA(launch_macros_ref(q_, sb_, pb_, d_f_[last_src_], d_macro_, launch_));
@@ -778,6 +786,28 @@ Status Engine::copy_force(void* fx, void* fy, void* fz) {
     TLBM_CUDA(cudaMemcpyAsync(o[k], d_force_[k], bytes, cudaMemcpyDeviceToHost, stream_));
   }
   TLBM_CUDA(cudaStreamSynchronize(stream_));
+  return Status::ok();
+}
+
+Status Engine::copy_outputs_async(void* const host[7]) {
+  TLBM_CUDA(cudaSetDevice(opt_.device));
+  TLBM_TRY(compute_outputs());
+  if (!copy_stream_) {
+    TLBM_CUDA(cudaStreamCreateWithFlags(&copy_stream_, cudaStreamNonBlocking));
+    TLBM_CUDA(cudaEventCreateWithFlags(&outputs_ready_, cudaEventDisableTiming));
+    TLBM_CUDA(cudaEventCreateWithFlags(&copies_done_, cudaEventDisableTiming));
+  }
+  TLBM_CUDA(cudaEventRecord(outputs_ready_, stream_));
+  TLBM_CUDA(cudaStreamWaitEvent(copy_stream_, outputs_ready_, 0));
+  const size_t bytes = static_cast<size_t>(n_) * ob_;
+  const void* dev[7] = {d_macro_[0], d_macro_[1], d_macro_[2], d_macro_[3],
+                        d_force_[0], d_force_[1], d_force_[2]};
+  for (int k = 0; k < 7; ++k) {
+    if (!host[k]) continue;
+    TLBM_CUDA(cudaMemcpyAsync(host[k], dev[k], bytes, cudaMemcpyDeviceToHost, copy_stream_));
+  }
+  TLBM_CUDA(cudaEventRecord(copies_done_, copy_stream_));
+  copies_pending_ = true;
   return Status::ok();
 }
 

@@ -50,6 +50,9 @@ class Engine {
   Status write_time_avg_data();
   Status copy_macros(void* ux, void* uy, void* uz, void* rho);
   Status copy_force(void* fx, void* fy, void* fz);
+  // ux, uy, uz, rho, fx, fy, fz (null entries skipped) of the last step, copied on a second
+  // stream while later steps run; the host buffers hold them after synchronize()
+  Status copy_outputs_async(void* const host[7]);
   Status copy_populations(int which, void* out);
   Status copy_adjacency(int32_t* out);
   Status mass(double* out);
@@ -100,6 +103,11 @@ class Engine {
   DevProblem pb_{};
   Launch launch_{};
   cudaStream_t stream_ = nullptr;
+  // copy_outputs_async: copies on copy_stream_ after outputs_ready_; the next recomputation of
+  // the output fields waits for copies_done_
+  cudaStream_t copy_stream_ = nullptr;
+  cudaEvent_t outputs_ready_ = nullptr, copies_done_ = nullptr;
+  bool copies_pending_ = false;
 
   uint8_t* d_type_ = nullptr;
   void* d_f_[2] = {nullptr, nullptr};  // [0] = fEven, [1] = fOdd
