@@ -792,10 +792,21 @@ Status Engine::copy_force(void* fx, void* fy, void* fz) {
 Status Engine::copy_outputs_async(void* const host[7]) {
   TLBM_CUDA(cudaSetDevice(opt_.device));
   TLBM_TRY(compute_outputs());
-  if (!copy_stream_) {
-    TLBM_CUDA(cudaStreamCreateWithFlags(&copy_stream_, cudaStreamNonBlocking));
-    TLBM_CUDA(cudaEventCreateWithFlags(&outputs_ready_, cudaEventDisableTiming));
-    TLBM_CUDA(cudaEventCreateWithFlags(&copies_done_, cudaEventDisableTiming));
+  if (!copy_stream_) {  // all three or none
+    cudaStream_t cs = nullptr;
+    cudaEvent_t ready = nullptr, done = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ready, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&done, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+      if (done) cudaEventDestroy(done);
+      if (ready) cudaEventDestroy(ready);
+      if (cs) cudaStreamDestroy(cs);
+      TLBM_CUDA(e);
+    }
+    copy_stream_ = cs;
+    outputs_ready_ = ready;
+    copies_done_ = done;
   }
   TLBM_CUDA(cudaEventRecord(outputs_ready_, stream_));
   TLBM_CUDA(cudaStreamWaitEvent(copy_stream_, outputs_ready_, 0));
