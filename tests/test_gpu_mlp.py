@@ -33,14 +33,17 @@ def test_gradient_matches_oracle():
     tr.set_params(p)
     loss, g = tr.loss_grad()
     loss_o, g_o, _ = M.forward_backward(p, X, t)
-    assert abs(loss - loss_o) <= 1e-2 * abs(loss_o)
+    assert abs(loss - loss_o) <= 1e-3 * abs(loss_o)
     err = np.linalg.norm(g - g_o) / np.linalg.norm(g_o)
     print("gradient relative L2 error vs oracle: %.2e" % err)
-    assert err <= 2e-2
+    # the kernels and the oracle round the same values to BF16; what differs is FP32 against
+    # FP64 accumulation and the special-function tanh (relative error below 2^-10.9), which
+    # moves an activation across a BF16 rounding boundary now and then (measured 1.7e-5)
+    assert err <= 1e-3
     # sub-range
     loss2, g2 = tr.loss_grad(100, 500)
     loss2_o, g2_o, _ = M.forward_backward(p, X[100:600], t[100:600])
-    assert np.linalg.norm(g2 - g2_o) / np.linalg.norm(g2_o) <= 2e-2
+    assert np.linalg.norm(g2 - g2_o) / np.linalg.norm(g2_o) <= 1e-3
 
 
 def test_training_reduces_loss_and_predict_matches_oracle():
@@ -205,8 +208,8 @@ def test_fused_tensor_core_closure_matches_oracle():
           "median %.2e" % (np.median(rel), np.percentile(rel, 99), np.median(rel_w)))
     # the kernel's activation rounds the special-function unit's FP32 tanh (relative error below
     # 2^-10.9) to BF16, which differs from the oracle's BF16 of the exact tanh by one BF16 ulp
-    # (2^-8 relative) where the two straddle a rounding boundary: ~1e-3 in y at most, ~1e-4 in
-    # the rate; FP32 round-off of the populations adds ~1e-5
-    assert np.median(rel) <= 5e-4
-    assert np.percentile(rel, 99) <= 3e-3
+    # (2^-8 relative) only where the two straddle a rounding boundary; FP32 round-off of the
+    # populations adds ~1e-7 to the rate (measured: median 3.5e-7, 99th percentile 4.5e-5)
+    assert np.median(rel) <= 1e-5
+    assert np.percentile(rel, 99) <= 1e-3
     assert np.median(rel_w) >= 10 * np.median(rel)
