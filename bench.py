@@ -490,6 +490,9 @@ def e2e(args, g, p, dist, plot_every=100):
         "h2d_bytes_per_step": round(n * 4 / steps),
         "d2h_bytes_per_step": round(d2h / steps),
         "seconds": {"total": round(dt, 4), "create": round(t_create, 4)},
+        "definition": "the reference's Estimated LPU/s (src/tLBM.cpp:69-73: nodes x steps over "
+                      "the time from construction to the end, dumps included), with the dumps "
+                      "read back to host memory instead of written to files",
         "includes": "lattice upload (int32 node types) + %d tlbm_step calls + write_data "
                     "fields read back every %d steps into page-locked host buffers, each copy "
                     "overlapping the steps after it"
