@@ -40,7 +40,7 @@ struct EnsembleChannel {
 
 // A tile: `cells` consecutive cells (threads x cells_per_thread) of one z-plane of one channel,
 // in the plane's x-fastest order, starting at plane index r0.
-struct EnsembleTile {
+struct alignas(16) EnsembleTile {  // one 16-byte load per tile
   int channel, z, r0, pad;
 };
 
