@@ -173,6 +173,9 @@ const char* tlbm_status_string(tlbm_status s);
 
 /* Bytes per value of output files and of the copy_* buffers below (8 or 4). */
 int tlbm_output_bytes(const tlbm_handle* h);
+/* The options the handle runs with, after tlbm.cfg and the defaults: *out is filled up to
+ * out->struct_size bytes (set it to sizeof(tlbm_options) first). */
+tlbm_status tlbm_get_options(const tlbm_handle* h, tlbm_options* out);
 int tlbm_num_speeds(const tlbm_handle* h);
 
 /* Macroscopic ux, uy, uz, rho of the last step in global node order (any pointer may be NULL). */

@@ -215,3 +215,11 @@ def test_host_alloc_arguments(lib):
     assert lib.tlbm_host_alloc(0, ctypes.byref(p)) == T.ERR_INVALID_ARGUMENT
     assert p.value is None
     assert lib.tlbm_host_free(None) == T.OK
+
+
+def test_get_options_arguments(lib):
+    """tlbm_get_options refuses a NULL handle or a bad struct_size without touching the device."""
+    o = T.Options()
+    o.struct_size = ctypes.sizeof(T.Options)
+    assert lib.tlbm_get_options(None, ctypes.byref(o)) == T.ERR_INVALID_ARGUMENT
+    assert lib.tlbm_get_options(None, None) == T.ERR_INVALID_ARGUMENT

@@ -7,6 +7,7 @@
   FP32 / BF16 / FP16 within the error budgets stated in each test.
 """
 
+import json
 import os
 import subprocess
 
@@ -62,9 +63,15 @@ def test_channel32_2000_steps_fp64_bit_exact(tmp_path):
 def test_tlbmexec_cli_fp32_bit_exact(tmp_path):
     """The tLBMexec command line (reference default precision) writes the reference's files."""
     write_case_inputs("q19_sphere_smag", str(tmp_path))
-    r = subprocess.run([B.EXE], cwd=str(tmp_path), capture_output=True, text=True, timeout=300)
+    metrics = str(tmp_path / "metrics.json")
+    r = subprocess.run([B.EXE, "--metrics", metrics], cwd=str(tmp_path), capture_output=True,
+                       text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     assert "Estimated LPU/s" in r.stdout and "Test complete." in r.stdout
+    m = json.load(open(metrics))
+    spec = CASES["q19_sphere_smag"]["spec"]
+    assert m["steps"] == spec["num_ts"] and m["lpu_s"] > 0 and m["elapsed_s"] > 0
+    assert m["precision"] == "f32" and m["arithmetic"] == "reference" and m["dumps"] >= 1
     want = CASES["q19_sphere_smag"]["outputs"]["f32"]
     got = output_digests(str(tmp_path))
     for f, h in want.items():

@@ -102,6 +102,7 @@ def library(path: str = LIB_PATH):
         "tlbm_get_last_error": (ctypes.c_char_p, [H]),
         "tlbm_status_string": (ctypes.c_char_p, [i32]),
         "tlbm_output_bytes": (i32, [H]),
+        "tlbm_get_options": (i32, [H, ctypes.POINTER(Options)]),
         "tlbm_num_speeds": (i32, [H]),
         "tlbm_copy_macros": (i32, [H, vp, vp, vp, vp]),
         "tlbm_copy_force": (i32, [H, vp, vp, vp]),

@@ -191,6 +191,16 @@ int tlbm_get_time_avg_flag(const tlbm_handle* h) {
 int tlbm_is_restart(const tlbm_handle* h) { return valid(h) ? h->engine->problem().restart_flag : -1; }
 int tlbm_get_cut_size(const tlbm_handle* h) { return valid(h) ? h->engine->cut_size() : -1; }
 
+tlbm_status tlbm_get_options(const tlbm_handle* h, tlbm_options* out) {
+  if (!valid(h) || !out || out->struct_size < static_cast<int>(sizeof(int)) ||
+      out->struct_size > static_cast<int>(sizeof(tlbm_options)))
+    return TLBM_ERR_INVALID_ARGUMENT;
+  const int n = out->struct_size;
+  std::memcpy(out, &h->engine->options(), static_cast<size_t>(n));
+  out->struct_size = n;
+  return TLBM_OK;
+}
+
 const char* tlbm_get_last_error(const tlbm_handle* h) {
   if (!h) return g_create_error.c_str();
   return h->error.c_str();

@@ -25,6 +25,7 @@
 #include "mlp.cuh"
 #include "mlp_kernels.h"
 #include "post.h"
+#include "trace.h"
 
 namespace tlbm {
 
@@ -264,6 +265,7 @@ void Engine::drop_graphs() {
 Status Engine::create(const tlbm_problem& prob, const int32_t* nd_type, const int32_t* parts,
                       int size, const std::string& workdir, const tlbm_options& opt,
                       Engine** out) {
+  TraceRange trace("tlbm_create");
   *out = nullptr;
   Engine* e = new (std::nothrow) Engine();
   if (!e) return Status::err(TLBM_ERR_NO_MEMORY, "out of host memory");
@@ -569,6 +571,7 @@ Status Engine::enqueue_step(int is_even) {
 }
 
 Status Engine::step(int is_even) {
+  TraceRange trace("tlbm_step");
   TLBM_CUDA(cudaSetDevice(opt_.device));
   return enqueue_step(is_even);
 }
@@ -596,6 +599,7 @@ Status Engine::build_graph(int parity) {
 }
 
 Status Engine::run(int first_ts, int nsteps) {
+  TraceRange trace("tlbm_run");
   TLBM_CUDA(cudaSetDevice(opt_.device));
   if (nsteps < 0) return Status::err(TLBM_ERR_INVALID_ARGUMENT, "nsteps < 0");
   int ts = first_ts;
@@ -620,6 +624,7 @@ Status Engine::run(int first_ts, int nsteps) {
 }
 
 Status Engine::time_steps(int first_ts, int nsteps, float* ms) {
+  TraceRange trace("tlbm_time_steps");
   TLBM_CUDA(cudaSetDevice(opt_.device));
   cudaEvent_t e0, e1;
   TLBM_CUDA(cudaEventCreate(&e0));
@@ -681,6 +686,7 @@ Status Engine::write_field(const std::string& name, const void* dev) {
 }
 
 Status Engine::write_data() {
+  TraceRange trace("tlbm_write_data");
   TLBM_CUDA(cudaSetDevice(opt_.device));
   if (workdir_.empty()) return Status::err(TLBM_ERR_IO, "no output directory");
   TLBM_TRY(compute_outputs());
@@ -698,6 +704,7 @@ Status Engine::write_data() {
 }
 
 Status Engine::write_time_avg_data() {
+  TraceRange trace("tlbm_write_time_avg_data");
   TLBM_CUDA(cudaSetDevice(opt_.device));
   if (prob_.time_avg_flag != 1)
     return Status::err(TLBM_ERR_INVALID_ARGUMENT, "time averaging is off (params.lbm line 15)");
@@ -764,6 +771,7 @@ Status Engine::write_processed(bool time_avg) {
 }
 
 Status Engine::copy_macros(void* ux, void* uy, void* uz, void* rho) {
+  TraceRange trace("tlbm_copy_macros");
   TLBM_CUDA(cudaSetDevice(opt_.device));
   TLBM_TRY(compute_outputs());
   void* o[4] = {ux, uy, uz, rho};
@@ -777,6 +785,7 @@ Status Engine::copy_macros(void* ux, void* uy, void* uz, void* rho) {
 }
 
 Status Engine::copy_force(void* fx, void* fy, void* fz) {
+  TraceRange trace("tlbm_copy_force");
   TLBM_CUDA(cudaSetDevice(opt_.device));
   TLBM_TRY(compute_outputs());
   void* o[3] = {fx, fy, fz};
@@ -790,6 +799,7 @@ Status Engine::copy_force(void* fx, void* fy, void* fz) {
 }
 
 Status Engine::copy_outputs_async(void* const host[7]) {
+  TraceRange trace("tlbm_copy_outputs_async");
   TLBM_CUDA(cudaSetDevice(opt_.device));
   TLBM_TRY(compute_outputs());
   if (!copy_stream_) {  // all three or none

@@ -46,6 +46,7 @@ class Engine {
   Status run(int first_ts, int nsteps);
   Status time_steps(int first_ts, int nsteps, float* ms);
   Status synchronize();
+  const tlbm_options& options() const { return opt_; }
   Status write_data();
   Status write_time_avg_data();
   Status copy_macros(void* ux, void* uy, void* uz, void* rho);

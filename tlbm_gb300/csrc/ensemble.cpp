@@ -5,6 +5,8 @@
 #include <algorithm>
 #include <cstring>
 
+#include "trace.h"
+
 namespace tlbm {
 
 #define TLBM_TRY(expr)         \
@@ -39,6 +41,7 @@ void Ensemble::drop_graphs() {
 
 Status Ensemble::create(int n, const tlbm_problem* probs, const int32_t* const* nd_types,
                         const tlbm_options& opt, Ensemble** out) {
+  TraceRange trace("tlbm_ensemble_create");
   *out = nullptr;
   Ensemble* e = new (std::nothrow) Ensemble();
   if (!e) return Status::err(TLBM_ERR_NO_MEMORY, "out of host memory");
@@ -211,6 +214,7 @@ Status Ensemble::enqueue(int is_even) {
 }
 
 Status Ensemble::run(int first_ts, int nsteps) {
+  TraceRange trace("tlbm_ensemble_run");
   TLBM_CUDA(cudaSetDevice(opt_.device));
   int ts = first_ts;
   if (nsteps >= 2) {
@@ -266,6 +270,7 @@ static const int kCandidates[][3] = {{64, 1, 1},  {128, 1, 1}, {256, 1, 1}, {64,
                                      {128, 1, 2}, {256, 1, 2}, {128, 1, 4}, {256, 1, 4}};
 
 Status Ensemble::autotune(int steps, int* bx, int* by, int* cpt) {
+  TraceRange trace("tlbm_ensemble_autotune");
   if (steps < 2) steps = 2;
   float best = 0.0f;
   int pick = -1;

@@ -6,8 +6,11 @@
 // dumps included, like the reference's MPI_Wtime pair.  Steps between two events (a progress
 // line or a dump) are issued as CUDA graph launches.
 //
-//   tLBMexec [-np N] [--precision f64|f32|bf16|f16] [--arithmetic reference|fast]
-//   -np N   job size the parts.lbm file was made for (default: accept any partition ids)
+//   tLBMexec [-np N] [--precision f64|f32|bf16|f16|bf16m] [--arithmetic reference|fast]
+//            [--metrics FILE]
+//   -np N           job size the parts.lbm file was made for (default: any partition ids)
+//   --metrics FILE  also write the run's figures as one JSON object (nodes, steps, dumps,
+//                   elapsed seconds, LPU/s, precision, arithmetic) to FILE
 #include <chrono>
 #include <climits>
 #include <cstdio>
@@ -26,6 +29,7 @@ static int fail(tlbm_handle* h, tlbm_status s) {
 int main(int argc, char* argv[]) {
   int size = INT_MAX / 2;
   bool have_opts = false;
+  std::string metrics;
   tlbm_options opt;
   tlbm_default_options(&opt);
   for (int i = 1; i < argc; ++i) {
@@ -45,8 +49,11 @@ int main(int argc, char* argv[]) {
       std::string v = argv[++i];
       have_opts = true;
       opt.arithmetic = (v == "fast") ? TLBM_ARITH_FAST : TLBM_ARITH_REFERENCE;
+    } else if (a == "--metrics" && i + 1 < argc) {
+      metrics = argv[++i];
     } else {
-      std::fprintf(stderr, "usage: tLBMexec [-np N] [--precision P] [--arithmetic A]\n");
+      std::fprintf(stderr,
+                   "usage: tLBMexec [-np N] [--precision P] [--arithmetic A] [--metrics FILE]\n");
       return 2;
     }
   }
@@ -61,6 +68,7 @@ int main(int argc, char* argv[]) {
   const int plot = tlbm_get_plot_freq(h);
   const int time_avg = tlbm_get_time_avg_flag(h);
 
+  int dumps = 0;
   auto t0 = std::chrono::steady_clock::now();
   int ts = 0;
   while (ts < num_ts) {
@@ -82,6 +90,7 @@ int main(int argc, char* argv[]) {
     if ((s = tlbm_step(h, ts % 2)) != TLBM_OK) return fail(h, s);
     if (((ts + 1) % plot == 0) && ((ts + 1) > warmup)) {
       if ((s = tlbm_write_data(h)) != TLBM_OK) return fail(h, s);
+      ++dumps;
     }
     ++ts;
   }
@@ -91,7 +100,27 @@ int main(int argc, char* argv[]) {
   std::printf("Test complete.\n");
   std::printf("Elapsed time: %g seconds \n", exec_time);
   const double nodes = static_cast<double>(tlbm_get_num_global_nodes(h));
-  std::printf("Estimated LPU/s = %g \n", nodes * static_cast<double>(num_ts) / exec_time);
+  const double lpus = nodes * static_cast<double>(num_ts) / exec_time;
+  std::printf("Estimated LPU/s = %g \n", lpus);
+  if (!metrics.empty()) {
+    static const char* kPrec[] = {"f64", "f32", "bf16", "f16", "bf16m"};
+    tlbm_options run_opt;
+    run_opt.struct_size = sizeof(run_opt);
+    if ((s = tlbm_get_options(h, &run_opt)) != TLBM_OK) return fail(h, s);
+    const int p = run_opt.precision >= 0 && run_opt.precision < 5 ? run_opt.precision : 1;
+    FILE* m = std::fopen(metrics.c_str(), "w");
+    if (!m) {
+      std::fprintf(stderr, "tLBMexec: cannot write %s\n", metrics.c_str());
+      tlbm_destroy(h);
+      return 1;
+    }
+    std::fprintf(m,
+                 "{\"nodes\": %.0f, \"steps\": %d, \"dumps\": %d, \"elapsed_s\": %.6f, "
+                 "\"lpu_s\": %.6g, \"precision\": \"%s\", \"arithmetic\": \"%s\"}\n",
+                 nodes, num_ts, dumps, exec_time, lpus, kPrec[p],
+                 run_opt.arithmetic == TLBM_ARITH_FAST ? "fast" : "reference");
+    std::fclose(m);
+  }
   if (time_avg == 1) {
     std::printf("Writing time average data.\n");
     if ((s = tlbm_write_time_avg_data(h)) != TLBM_OK) return fail(h, s);
