@@ -145,7 +145,13 @@ def test_closure_pipeline_small():
     assert (not out["none"]["finite"]) or err(out["learned"]) <= err(out["none"])
 
 
-def test_fused_tensor_core_closure_matches_oracle():
+# lattice weights by |e|^2 (include/D3Q{15,19,27}LatticeStructure.hpp), as the kernels use them
+WEIGHTS = {15: {0: 2 / 9, 1: 1 / 9, 3: 1 / 72}, 19: {0: 1 / 3, 1: 1 / 18, 2: 1 / 36},
+           27: {0: 8 / 27, 1: 2 / 27, 2: 1 / 54, 3: 1 / 216}}
+
+
+@pytest.mark.parametrize("q", [19, 15, 27])
+def test_fused_tensor_core_closure_matches_oracle(q):
     """One step of the fused collide kernel with a random network, from a non-equilibrium state
     on an all-fluid periodic box, against the closure computed in numpy: moments, Pi_neq,
     normalised features, the BF16-rounded network (mlp_oracle), tau = 3 (nu + s y) + 1/2 and the
@@ -154,7 +160,7 @@ def test_fused_tensor_core_closure_matches_oracle():
     most nodes by ~1e-4."""
     nx, ny, nz = 64, 8, 6
     g = G.Geometry(nx, ny, nz, np.zeros(nx * ny * nz, np.int32))
-    p = G.params_lattice_units(g, "D3Q19", 0.05, 60.0, 6.0, 10)
+    p = G.params_lattice_units(g, "D3Q%d" % q, 0.05, 60.0, 6.0, 10)
     p.omega = 1.6
     n = g.num_nodes
     part = T.TLBMPartition.from_arrays(T.problem_from_params(p), g.nd_type, precision="f32",
@@ -163,12 +169,12 @@ def test_fused_tensor_core_closure_matches_oracle():
     part.load_restart(rng.uniform(-0.04, 0.04, n), rng.uniform(-0.04, 0.04, n),
                       rng.uniform(-0.04, 0.04, n), rng.uniform(0.99, 1.01, n))
     part.run(0, 1)
-    f = part.populations(0).reshape(n, 19).astype(np.float64)  # input of the next step
+    f = part.populations(0).reshape(n, q).astype(np.float64)  # input of the next step
     # lattice vectors from the neighbour table (push target of an interior node)
     c = 1 + nx + nx * ny
-    tgt = part.adjacency().reshape(n, 19)[c]
+    tgt = part.adjacency().reshape(n, q)[c]
     e = np.stack([tgt % nx - 1, (tgt // nx) % ny - 1, tgt // (nx * ny) - 1], axis=1)
-    w = np.array([{0: 1 / 3, 1: 1 / 18, 2: 1 / 36}[int(k)] for k in (e * e).sum(1)], np.float32)
+    w = np.array([WEIGHTS[q][int(k)] for k in (e * e).sum(1)], np.float32)
     w = w.astype(np.float64)
     rho = f.sum(1)
     u = (f @ e) / rho[:, None]
@@ -177,8 +183,8 @@ def test_fused_tensor_core_closure_matches_oracle():
     d = f - feq
     pairs = [(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]
     pi = np.stack([(d * (e[:, a] * e[:, b])[None, :]).sum(1) for a, b in pairs], axis=1)
-    q = np.sqrt((pi[:, :3] ** 2).sum(1) + 2 * (pi[:, 3:] ** 2).sum(1))
-    raw = np.concatenate([pi, (rho - 1)[:, None], q[:, None]], axis=1)
+    pi_norm = np.sqrt((pi[:, :3] ** 2).sum(1) + 2 * (pi[:, 3:] ** 2).sum(1))
+    raw = np.concatenate([pi, (rho - 1)[:, None], pi_norm[:, None]], axis=1)
     shift = raw.mean(0).astype(np.float32)
     scale = (1.0 / raw.std(0)).astype(np.float32)
     x = ((raw.astype(np.float32) - shift) * scale).astype(np.float32)
@@ -191,10 +197,10 @@ def test_fused_tensor_core_closure_matches_oracle():
     assert tau.min() > tau_min and np.ptp(tau) > 1e-3
     part.set_closure_mlp(params, scale, shift, out_scale, tau_min)
     part.run(1, 1)
-    got = part.populations(1).reshape(n, 19).astype(np.float64)
+    got = part.populations(1).reshape(n, q).astype(np.float64)
 
     def rate_error(tau_of_cell):
-        # the relaxation rate each node applied (least squares over its 19 speeds) against 1/tau
+        # the relaxation rate each node applied (least squares over its q speeds) against 1/tau
         om = ((f - got) * d).sum(1) / (d * d).sum(1)
         return np.abs(om * tau_of_cell - 1.0)
 
@@ -204,8 +210,8 @@ def test_fused_tensor_core_closure_matches_oracle():
     wrong[M.OW3:M.OB3] *= 1.25
     _, _, y_w = M.forward_backward(wrong, x, np.zeros(n))
     rel_w = rate_error(np.maximum(3.0 * (nu + out_scale * y_w) + 0.5, tau_min))
-    print("fused closure step: rate error median %.2e, 99th pct %.2e; perturbed network "
-          "median %.2e" % (np.median(rel), np.percentile(rel, 99), np.median(rel_w)))
+    print("fused closure step D3Q%d: rate error median %.2e, 99th pct %.2e; perturbed network "
+          "median %.2e" % (q, np.median(rel), np.percentile(rel, 99), np.median(rel_w)))
     # the kernel's activation rounds the special-function unit's FP32 tanh (relative error below
     # 2^-10.9) to BF16, which differs from the oracle's BF16 of the exact tanh by one BF16 ulp
     # (2^-8 relative) only where the two straddle a rounding boundary; FP32 round-off of the
