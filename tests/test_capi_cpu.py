@@ -223,3 +223,13 @@ def test_get_options_arguments(lib):
     o.struct_size = ctypes.sizeof(T.Options)
     assert lib.tlbm_get_options(None, ctypes.byref(o)) == T.ERR_INVALID_ARGUMENT
     assert lib.tlbm_get_options(None, None) == T.ERR_INVALID_ARGUMENT
+
+
+def test_host_empty_fails_loudly_without_a_device(lib):
+    """Page-locked host memory needs the CUDA driver: without a GPU, host_empty raises."""
+    import shutil
+    smi = shutil.which("nvidia-smi")
+    if smi and subprocess.run([smi], capture_output=True).returncode == 0:
+        pytest.skip("a GPU is present")
+    with pytest.raises(T.TLBMError):
+        T.host_empty(16, np.float32)
