@@ -233,3 +233,17 @@ def test_host_empty_fails_loudly_without_a_device(lib):
         pytest.skip("a GPU is present")
     with pytest.raises(T.TLBMError):
         T.host_empty(16, np.float32)
+
+
+@pytest.mark.parametrize("cfg,word", [("arithmetic exact\n", "arithmetic"),
+                                      ("colour blue\n", "unknown key"),
+                                      ("precision bf16\narithmetic reference\n", ""),
+                                      ("precision bf16m\narithmetic reference\n", "")])
+def test_config_file_refusals(lib, tmp_path, cfg, word):
+    """tlbm.cfg is parsed and checked before any device work: unknown keys and values, and
+    16-bit storage with the reference arithmetic (which has no 16-bit form), are refused."""
+    small_inputs(tmp_path)
+    open(tmp_path / "tlbm.cfg", "w").write(cfg)
+    st, msg = create_status(lib, tmp_path)
+    assert st == T.ERR_INVALID_ARGUMENT and msg
+    assert word in msg
