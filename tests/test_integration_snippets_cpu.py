@@ -39,3 +39,21 @@ def test_python_stub_is_valid():
     assert src
     for b in src:
         compile(b, "INTEGRATION.md", "exec")
+
+
+def test_header_is_strict_c(tmp_path):
+    """include/tlbm.h is a C header (cgo, ctypes and C callers): it compiles as pedantic C99
+    and a C program links against the engine with it."""
+    cc = shutil.which("gcc")
+    if not cc:
+        pytest.skip("gcc not available")
+    B.build()
+    f = tmp_path / "use.c"
+    f.write_text('#include "tlbm.h"\n'
+                 "int main(void) { tlbm_options o; tlbm_default_options(&o);\n"
+                 "  return o.struct_size > 0 ? 0 : 1; }\n")
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic",
+                        "-I" + os.path.join(B.REPO, "include"), str(f),
+                        "-L" + os.path.dirname(B.LIB), "-ltlbm_gb300", "-o", str(tmp_path / "use")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
