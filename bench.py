@@ -224,7 +224,9 @@ def traffic_per_cell(lattice, precision):
 # ----------------------------------------------------------------------------- arms
 
 
-def cpu_baseline(g, p, steps=20, warmup=2):
+def cpu_baseline(g, p, seconds=10.0, chunk=10, warmup=2):
+    """The CPU restatement of the reference timestep on all host cores, on a z-slab of the
+    workload, timed over whole chunks of steps until `seconds` of work have passed."""
     sys.path.insert(0, os.path.join(HERE, "tests"))
     import oracle_lib
 
@@ -234,9 +236,14 @@ def cpu_baseline(g, p, steps=20, warmup=2):
     o = oracle_lib.Oracle(q, 1, p.cs, p.rho_lbm, p.u_lbm, p.omega, g.nx, g.ny, nz, nd,
                           prec="f64", threads=threads)
     o.run(warmup)
+    steps = 0
     t0 = time.perf_counter()
-    o.run(steps)
-    dt = time.perf_counter() - t0
+    while True:
+        o.run(chunk)
+        steps += chunk
+        dt = time.perf_counter() - t0
+        if dt >= seconds:
+            break
     o.close()
     cells = g.nx * g.ny * nz
     return {
@@ -245,9 +252,9 @@ def cpu_baseline(g, p, steps=20, warmup=2):
         "cores": threads,
         "kind": "port",
         "sample": "%dx%dx%d slab of the same sphere pack (%s FP64 BGK+Smagorinsky), %d warm-up + "
-                  "%d timed steps of the C restatement of the reference timestep "
+                  "%d timed steps (%.1f s) of the C restatement of the reference timestep "
                   "(AoS push, int32 neighbour table), OpenMP over nodes"
-                  % (g.nx, g.ny, nz, p.lattice, warmup, steps),
+                  % (g.nx, g.ny, nz, p.lattice, warmup, steps, dt),
     }
 
 
