@@ -247,3 +247,21 @@ def test_config_file_refusals(lib, tmp_path, cfg, word):
     st, msg = create_status(lib, tmp_path)
     assert st == T.ERR_INVALID_ARGUMENT and msg
     assert word in msg
+
+
+def test_python_mirror_checks_array_sizes_before_the_abi(lib):
+    """The C ABI reads a fixed number of values through each pointer; the Python mirror refuses
+    arrays of the wrong length before any call (a short array would be read out of bounds)."""
+    g = G.sphere_in_box(8, 8, 12, 2, 4, 4, 5)
+    p = G.params_lattice_units(g, "D3Q19", 0.04, 20.0, 4.0, 10)
+    prob = T.problem_from_params(p)
+    with pytest.raises(ValueError, match="nd_type"):
+        T.TLBMPartition.from_arrays(prob, g.nd_type[:-1])
+    with pytest.raises(ValueError, match="parts"):
+        T.TLBMPartition.from_arrays(prob, g.nd_type, parts=np.zeros(5, np.int32))
+    with pytest.raises(ValueError, match="nd_types"):
+        T.Ensemble([prob, prob], [g.nd_type, g.nd_type[:10]])
+    with pytest.raises(ValueError, match="node-type arrays"):
+        T.Ensemble([prob, prob], [g.nd_type])
+    a = T._sized(np.arange(6).reshape(2, 3), np.float32, 6, "x")
+    assert a.shape == (6,) and a.dtype == np.float32 and a.flags.c_contiguous

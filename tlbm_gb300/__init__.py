@@ -193,6 +193,15 @@ def _check(status: int, handle=None) -> None:
         raise TLBMError(status, msg or L.tlbm_status_string(status).decode())
 
 
+def _sized(a, dtype, n: int, what: str) -> np.ndarray:
+    """`a` as a contiguous 1-D array of n values of dtype: the C ABI reads exactly n values
+    through a bare pointer, so a wrong length is refused here instead of read out of bounds."""
+    out = np.ascontiguousarray(a, dtype=dtype).reshape(-1)
+    if out.size != n:
+        raise ValueError("%s: %d values given, %d expected" % (what, out.size, n))
+    return out
+
+
 class TLBMPartition:
     """The reference's TLBM_Partition over the GPU engine (one process, whole lattice)."""
 
@@ -225,8 +234,11 @@ class TLBMPartition:
                     precision="f64", arithmetic=None, block_x=0, block_y=0, device=0,
                     rbgk=False, mrt=False, ghost_rate=0.0):
         L = library()
-        nd = np.ascontiguousarray(nd_type, dtype=np.int32)
-        pp = None if parts is None else np.ascontiguousarray(parts, dtype=np.int32)
+        cells = int(problem.nx) * int(problem.ny) * int(problem.nz)
+        if cells <= 0:
+            raise ValueError("lattice %d x %d x %d" % (problem.nx, problem.ny, problem.nz))
+        nd = _sized(nd_type, np.int32, cells, "nd_type")
+        pp = None if parts is None else _sized(parts, np.int32, cells, "parts")
         o = options(precision, arithmetic, block_x, block_y, device, rbgk, mrt, ghost_rate)
         h = ctypes.c_void_p()
         _check(L.tlbm_create_from_arrays(ctypes.byref(problem), nd.ctypes.data,
@@ -343,7 +355,8 @@ class TLBMPartition:
 
     def load_restart(self, ux, uy, uz, rho) -> None:
         """Populations = equilibrium of the given fields (load_restart_data)."""
-        arrs = [np.ascontiguousarray(a, dtype=np.float32).reshape(-1) for a in (ux, uy, uz, rho)]
+        arrs = [_sized(a, np.float32, self.n, name)
+                for a, name in ((ux, "ux"), (uy, "uy"), (uz, "uz"), (rho, "rho"))]
         _check(self._L.tlbm_load_restart(self._h, *[a.ctypes.data for a in arrs]), self._h)
 
     def set_inlet_profile(self, uz) -> None:
@@ -351,7 +364,8 @@ class TLBMPartition:
         if uz is None:
             _check(self._L.tlbm_set_inlet_profile(self._h, None), self._h)
             return
-        self._inlet = np.ascontiguousarray(uz, dtype=np.float64).reshape(-1)
+        nx, ny, _ = self._shape()
+        self._inlet = _sized(uz, np.float64, nx * ny, "inlet profile")
         _check(self._L.tlbm_set_inlet_profile(self._h, self._inlet.ctypes.data), self._h)
 
     def set_closure_mlp(self, params, scale, shift, out_scale: float, tau_min: float) -> None:
@@ -359,9 +373,9 @@ class TLBMPartition:
         if params is None:
             _check(self._L.tlbm_set_closure_mlp(self._h, None, None, None, 0.0, 0.0), self._h)
             return
-        p = np.ascontiguousarray(params, dtype=np.float32)
-        s = np.ascontiguousarray(scale, dtype=np.float32)
-        h = np.ascontiguousarray(shift, dtype=np.float32)
+        p = _sized(params, np.float32, self._L.tlbm_mlp_num_params(), "params")
+        s = _sized(scale, np.float32, 8, "scale")
+        h = _sized(shift, np.float32, 8, "shift")
         _check(self._L.tlbm_set_closure_mlp(self._h, p.ctypes.data, s.ctypes.data, h.ctypes.data,
                                             float(out_scale), float(tau_min)), self._h)
 
@@ -477,7 +491,10 @@ class Ensemble:
         self._L = L
         n = len(problems)
         self._probs = (Problem * n)(*problems)
-        self._nd = [np.ascontiguousarray(a, dtype=np.int32) for a in nd_types]
+        if len(nd_types) != n:
+            raise ValueError("%d problems and %d node-type arrays" % (n, len(nd_types)))
+        self._nd = [_sized(a, np.int32, int(pr.nx) * int(pr.ny) * int(pr.nz), "nd_types[%d]" % k)
+                    for k, (a, pr) in enumerate(zip(nd_types, problems))]
         ptrs = (ctypes.c_void_p * n)(*[a.ctypes.data for a in self._nd])
         o = options(precision, "fast", block_x, block_y, device)
         self._h = ctypes.c_void_p()
@@ -563,7 +580,7 @@ class MlpTrainer:
             raise TLBMError(st, self._L.tlbm_mlp_last_error(self._h).decode())
 
     def set_params(self, p):
-        p = np.ascontiguousarray(p, dtype=np.float32)
+        p = _sized(p, np.float32, self.n_params, "params")
         self._check(self._L.tlbm_mlp_set_params(self._h, p.ctypes.data))
 
     def params(self):
