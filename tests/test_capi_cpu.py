@@ -265,3 +265,17 @@ def test_python_mirror_checks_array_sizes_before_the_abi(lib):
         T.Ensemble([prob, prob], [g.nd_type])
     a = T._sized(np.arange(6).reshape(2, 3), np.float32, 6, "x")
     assert a.shape == (6,) and a.dtype == np.float32 and a.flags.c_contiguous
+
+
+def test_create_from_arrays_null_arguments(lib):
+    g = G.sphere_in_box(8, 8, 12, 2, 4, 4, 5)
+    p = G.params_lattice_units(g, "D3Q19", 0.04, 20.0, 4.0, 10)
+    prob = T.problem_from_params(p)
+    o = T.options("f64")
+    h = ctypes.c_void_p()
+    assert lib.tlbm_create_from_arrays(ctypes.byref(prob), None, None, None, ctypes.byref(o),
+                                       ctypes.byref(h)) == T.ERR_INVALID_ARGUMENT
+    assert h.value is None
+    assert lib.tlbm_create_from_arrays(None, g.nd_type.ctypes.data, None, None, ctypes.byref(o),
+                                       ctypes.byref(h)) == T.ERR_INVALID_ARGUMENT
+    assert b"NULL" in lib.tlbm_get_last_error(None)
