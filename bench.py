@@ -457,9 +457,17 @@ def extras(args, g, p, dist):
     res = studies.precision_study(gs, ps, 1000, forms=("f64-fast", "f32", "f16", "bf16", "bf16m"),
                                   device=dist.local)
     out["precision_1000_steps_256x128x128"] = {
-        k: {kk: (round(vv, 9) if isinstance(vv, float) else vv) for kk, vv in v.items()}
-        for k, v in res.items()}
+        k: {kk: fmt_study(kk, vv) for kk, vv in v.items()} for k, v in res.items()}
     return out
+
+
+def fmt_study(key, v):
+    """Study values as 4 significant digits (errors down to 1e-16 stay visible); MLUPS to 0.1."""
+    if not isinstance(v, float):
+        return v
+    if key == "mlups":
+        return round(v, 1)
+    return float("%.3e" % v)
 
 
 def e2e(args, g, p, dist, plot_every=100):
@@ -482,9 +490,11 @@ def e2e(args, g, p, dist, plot_every=100):
     d2h = 0
     for ts in range(steps):
         part.take_LBM_time_step(ts % 2)
-        if (ts + 1) % plot_every == 0:
+        if (ts + 1) % plot_every == 0 or ts == steps - 1:
             # the fields of this step, copied while the next steps run (the host link ramps
-            # up slowly after a stretch without traffic: ~0.1 s for the first 1.9 GB)
+            # up slowly after a stretch without traffic: ~0.1 s for the first 1.9 GB); the
+            # last step's fields are always read back, so every run ends with its result in
+            # host memory whatever the step count
             fields = part.outputs_async(host)
             d2h += sum(a.nbytes for a in fields)
     part.synchronize()  # every step and every copy done
@@ -500,10 +510,10 @@ def e2e(args, g, p, dist, plot_every=100):
         "definition": "the reference's Estimated LPU/s (src/tLBM.cpp:69-73: nodes x steps over "
                       "the time from construction to the end, dumps included), with the dumps "
                       "read back to host memory instead of written to files",
-        "includes": "lattice upload (int32 node types) + %d tlbm_step calls + write_data "
-                    "fields read back every %d steps into page-locked host buffers, each copy "
-                    "overlapping the steps after it"
-                    % (steps, plot_every),
+        "includes": "lattice upload (int32 node types, once per run) + %d tlbm_step calls + "
+                    "write_data fields (7 x %d values) read back after every %dth step and after "
+                    "the last one into page-locked host buffers, each copy overlapping the steps "
+                    "after it" % (steps, n, plot_every),
     }
 
 

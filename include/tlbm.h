@@ -338,9 +338,12 @@ const char* tlbm_ensemble_last_error(const tlbm_ensemble* e);
  * `precision`, 16-bit kinds holding f - w) and `mass` (device memory, one double), and the
  * partial sums go to a static device array of 512 KiB that every GPU loading the library keeps
  * until exit.  Limit: n_cells <= 67108864 (65536 partials of 1024 cells); larger inputs return
- * TLBM_ERR_OUT_OF_RANGE and launch nothing.  The first call on a device looks up that array's
- * address (make it before any stream capture).  Asynchronous on `stream` (a cudaStream_t; NULL
- * is the default stream).  All calls share the array: calls that overlap on the GPU race. */
+ * TLBM_ERR_OUT_OF_RANGE and launch nothing.  Each call on a stream that is not being captured
+ * looks up that array's address on the current device (make the first call on a device before
+ * any stream capture).  Asynchronous on `stream` (a cudaStream_t; NULL is the default stream).
+ * All calls share the array: calls that overlap on the GPU race.  The sum is not checked: a
+ * diverged run yields NaN or Inf in *mass, not TLBM_ERR_NUMERIC as from tlbm_mass, so test it
+ * with isfinite after synchronizing. */
 tlbm_status tlbm_mass_static(int q, int precision, int64_t n_cells, const void* populations,
                              double* mass, void* stream);
 

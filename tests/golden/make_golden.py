@@ -1,9 +1,8 @@
 #!/usr/bin/env python3
 """Regenerate the golden fixtures in this directory from the reference itself.
 
-Run in a checkout where the reference tree is available (default ``/root/reference``,
-override with ``TLBM_REFERENCE``) after ``make -C oracle ref`` has built the reference
-solver (``oracle/_ref/tLBMexec_f32`` and ``tLBMexec_f64``) from its own sources.
+Run with ``TLBM_REFERENCE`` naming a reference checkout (required), after
+``make -C oracle ref REF=$TLBM_REFERENCE`` has built the reference solver (``oracle/_ref/tLBMexec_f32`` and ``tLBMexec_f64``) from its own sources.
 
 For every case this script
 
@@ -37,7 +36,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("TLBM_REFERENCE", "/root/reference")
+REF = os.environ.get("TLBM_REFERENCE", "")
+if not os.path.isdir(os.path.join(REF, "python")):
+    sys.exit("make_golden.py: set TLBM_REFERENCE to a reference checkout")
 REF_PY = os.path.join(REF, "python")
 EXE = {p: os.path.join(REPO, "oracle", "_ref", "tLBMexec_" + p) for p in ("f32", "f64")}
 

@@ -111,4 +111,7 @@ def main(reference):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("TLBM_REFERENCE", "")
+    if not os.path.isdir(os.path.join(ref, "python")):
+        sys.exit("make_post_golden.py: pass the reference checkout (or set TLBM_REFERENCE)")
+    main(ref)

@@ -58,6 +58,33 @@ def test_mass_static_matches_tlbm_mass_on_two_calls(precision):
     part.close()
 
 
+# D3Q19 weights as the kernels hold them: float literals (include/D3Q19LatticeStructure.hpp)
+W19 = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12, np.float32).astype(np.float64)
+
+
+@pytest.mark.parametrize("precision", ["bf16", "f16"])
+def test_mass_static_shifted_storage_on_two_calls(precision):
+    """16-bit kinds store f - w_i: the sum adds w_i back per population.  The caller's array
+    holds the 16-bit remainders of a seeded non-equilibrium state; the result must equal the
+    FP64 sum of float(stored) + w_i on two calls with different contents."""
+    torch = pytest.importorskip("torch")
+    fn = entry()
+    q, n = 19, 40 * 24 * 30 + 7  # a partial last block
+    dt = torch.bfloat16 if precision == "bf16" else torch.float16
+    out = torch.full((1,), -1.0, dtype=torch.float64, device="cuda")
+    rng = np.random.default_rng(5)
+    for call in range(2):
+        f = W19[:, None] * rng.uniform(0.9, 1.1, size=(q, n))
+        stored = torch.from_numpy(f - W19[:, None]).to(dt)
+        want = float((stored.to(torch.float64).numpy() + W19[:, None]).sum())
+        dev = stored.to("cuda")
+        torch.cuda.synchronize()
+        assert fn(q, T.PREC[precision], n, dev.data_ptr(), out.data_ptr(), None) == T.OK
+        torch.cuda.synchronize()
+        got = float(out.item())
+        assert abs(got - want) <= 1e-12 * abs(want), (call, got, want)
+
+
 def test_mass_static_rejects_sizes_beyond_its_scratch():
     torch = pytest.importorskip("torch")
     fn = entry()

@@ -10,13 +10,16 @@
 // Its scratch is g_mass_scratch below: kMassStaticMaxBlocks doubles (512 KiB), a file-scope
 // __device__ array that is part of this library's device image, so every GPU that loads the
 // library holds it until the process exits.  In host code the name g_mass_scratch is only a
-// stand-in for the symbol, not a device address: the first call on each device, with that
-// device current, asks the runtime for the array's device address (cudaGetSymbolAddress) and
-// keeps it for later calls.  Make that first call before any stream capture.
+// stand-in for the symbol, not a device address: each call, with the device current, asks the
+// runtime for the array's device address (cudaGetSymbolAddress) when its stream is not being
+// captured, and keeps it per device for a call made during a capture.  Make the first call on
+// a device before any stream capture.
 //
 // All calls share the array and it keeps the last call's partial sums.  Every call writes each
 // partial it later reads, so nothing has to be cleared between calls; calls that overlap on the
 // GPU (two streams, or two host threads) race on the array and must be ordered by the caller.
+// The sum is not checked: a diverged run yields NaN or Inf in *mass (tlbm_mass returns
+// TLBM_ERR_NUMERIC instead), so the caller tests it with isfinite after synchronizing.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -123,10 +126,16 @@ extern "C" tlbm_status tlbm_mass_static(int q, int precision, int64_t n_cells,
   if (nb64 > kMassStaticMaxBlocks) return TLBM_ERR_OUT_OF_RANGE;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return TLBM_ERR_CUDA;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // Outside stream capture the array's address is looked up on every call, so an address kept
+  // from before a cudaDeviceReset (or from another context on this device) is never used; a
+  // call on a capturing stream uses the address of the last call outside capture.
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) return TLBM_ERR_CUDA;
   double* scratch = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_ptr[dev]) {
+    if (cap == cudaStreamCaptureStatusNone) {
       void* p = nullptr;
       const cudaError_t e = cudaGetSymbolAddress(&p, g_mass_scratch);
       if (e != cudaSuccess || !p) return TLBM_ERR_CUDA;
@@ -134,11 +143,11 @@ extern "C" tlbm_status tlbm_mass_static(int q, int precision, int64_t n_cells,
     }
     scratch = g_scratch_ptr[dev];
   }
+  if (!scratch) return TLBM_ERR_CUDA;
   const int store = precision == TLBM_PREC_F64   ? kStoreF64
                     : precision == TLBM_PREC_F32 ? kStoreF32
                     : precision == TLBM_PREC_BF16 ? kStoreBF16
                                                   : kStoreF16;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int nb = static_cast<int>(nb64);
   cudaError_t e = dispatch_partial(q, store, populations, n_cells, nb, scratch, s);
   if (e == cudaSuccess) {
