@@ -47,7 +47,7 @@ def parse_args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--lattice", default="D3Q19")
     ap.add_argument("--precision", default="f64", choices=["f64", "f32", "bf16", "f16", "bf16m"])
-    ap.add_argument("--arithmetic", default="fast", choices=["fast", "reference"])
+    ap.add_argument("--arithmetic", default="fast", choices=["fast", "fast-fp64", "reference"])
     ap.add_argument("--nx", type=int, default=512)
     ap.add_argument("--ny", type=int, default=256)
     ap.add_argument("--nz", type=int, default=256)
@@ -447,6 +447,8 @@ def extras(args, g, p, dist):
     for lat, prec in (("D3Q27", "f64"), ("D3Q19", "f32"), ("D3Q27", "f32"), ("D3Q19", "bf16"),
                       ("D3Q19", "f16"), ("D3Q19", "bf16m")):
         out["lines"].append(variant_line(g, p, lat, prec, "fast", 50, dist.local))
+    out["lines"].append(variant_line(g, p, "D3Q19", "f64", "fast-fp64", 20, dist.local))
+    out["lines"].append(variant_line(g, p, "D3Q27", "f64", "fast-fp64", 20, dist.local))
     out["lines"].append(variant_line(g, p, "D3Q19", "f64", "reference", 20, dist.local))
     out["ensemble"] = ensemble_line(dist.local)
     out["closure"] = closure_line(g, p, dist.local)
@@ -454,8 +456,8 @@ def extras(args, g, p, dist):
     # reference-exact run (byte-identical to the CPU reference)
     gs = G.random_sphere_pack(256, 128, 128, 4.0, 12.0, 0.7, seed=args.seed)
     ps = G.params_lattice_units(gs, "D3Q19", 0.04, 200.0, gs.lo, 1000, cs=0.1, rho_lbm=1.0)
-    res = studies.precision_study(gs, ps, 1000, forms=("f64-fast", "f32", "f16", "bf16", "bf16m"),
-                                  device=dist.local)
+    res = studies.precision_study(gs, ps, 1000, forms=("f64-fast", "f64-fast-fp64", "f32", "f16",
+                                                       "bf16", "bf16m"), device=dist.local)
     out["precision_1000_steps_256x128x128"] = {
         k: {kk: fmt_study(kk, vv) for kk, vv in v.items()} for k, v in res.items()}
     return out

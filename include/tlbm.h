@@ -83,7 +83,12 @@ typedef struct tlbm_options {
                       order at mrt_ghost_rate (fast arithmetic only) */
   float mrt_ghost_rate; /* ghost-moment rate in (0, 2), a float; <= 0 selects 1.2.  The rate
                            omega gives BGK, 1 the regularised collision. */
-  int reserved[6];
+  int f64_pipe;    /* TLBM_PREC_F64 with TLBM_ARITH_FAST: 0 (default) collides fluid nodes in
+                      exact 64-bit fixed point (double-float for the Smagorinsky rate) and rounds
+                      each result once to double, so no FP64 instruction runs on the fluid path;
+                      1 collides them in FP64 arithmetic on the FP64 pipe, as boundary nodes
+                      always are.  Both meet the same bar against the reference arithmetic. */
+  int reserved[5];
 } tlbm_options;
 
 /* The 23 values of params.lbm in file order (Problem, include/Problem.h:18-40). */

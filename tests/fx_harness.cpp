@@ -1,0 +1,202 @@
+// fx_harness.cpp -- host check of physics_fx.cuh (the fixed-point FP64-storage collision).
+//
+//   fx_harness Q SMAG N SEED
+//
+// For N random near-equilibrium cells (rho in [0.8, 1.2], |u_a| <= 0.1, non-equilibrium parts up
+// to 2e-3 w_i) it collides each cell with fx::fluid_collide and with a long-double evaluation of
+// the reference's formulas (include/LatticeStructure.hpp:70-163: moments, equilibrium with the
+// reference's weights, Smagorinsky rate, BGK relaxation), and prints the largest difference in
+// ulps of the result and the share of results that are not the nearest double.  It also checks
+// the exact double <-> Q4.59 conversions and the range guards.  Exit status 1 on a failed check.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <random>
+
+#include "../tlbm_gb300/csrc/physics_fx.cuh"
+
+using namespace tlbm;
+using LD = long double;
+
+template <class L>
+LD w_of(int i) {
+  return static_cast<LD>(static_cast<double>(L::wlit(i)));
+}
+
+// reference collision in long double, result rounded to double
+template <class L>
+void collide_exact(const double (&f)[L::Q], bool smag, double omega, double cs, double (&out)[L::Q]) {
+  constexpr int Q = L::Q;
+  LD rho = 0, jx = 0, jy = 0, jz = 0;
+  for (int i = 0; i < Q; ++i) {
+    rho += f[i];
+    jx += L::ex(i) * static_cast<LD>(f[i]);
+    jy += L::ey(i) * static_cast<LD>(f[i]);
+    jz += L::ez(i) * static_cast<LD>(f[i]);
+  }
+  const LD ux = jx / rho, uy = jy / rho, uz = jz / rho;
+  LD feq[Q];
+  for (int i = 0; i < Q; ++i) {
+    const LD cu = 3 * (L::ex(i) * ux + L::ey(i) * uy + L::ez(i) * uz);
+    feq[i] = w_of<L>(i) * rho * (1 + cu + 0.5L * cu * cu - 1.5L * (ux * ux + uy * uy + uz * uz));
+  }
+  LD om = omega;
+  if (smag) {
+    LD s[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = 0; i < Q; ++i) {
+      const LD d = f[i] - feq[i];
+      const int ex = L::ex(i), ey = L::ey(i), ez = L::ez(i);
+      s[0] += ex * ex * d;
+      s[1] += ey * ey * d;
+      s[2] += ez * ez * d;
+      s[3] += ex * ey * d;
+      s[4] += ex * ez * d;
+      s[5] += ey * ez * d;
+    }
+    const LD nu = (1 / static_cast<LD>(omega) - 0.5L) / 3;
+    LD p = std::sqrt(s[0] * s[0] + s[1] * s[1] + s[2] * s[2] +
+                     2 * (s[3] * s[3] + s[4] * s[4] + s[5] * s[5]));
+    p *= cs;
+    p = std::sqrt(p + nu * nu) - nu;
+    om = 1 / (3 * (nu + p / 6) + 0.5L);
+  }
+  for (int i = 0; i < Q; ++i) out[i] = static_cast<double>(f[i] - om * (f[i] - feq[i]));
+}
+
+double ulps(double a, double b) {
+  if (a == b) return 0;
+  const double u = std::nextafter(std::fabs(b), INFINITY) - std::fabs(b);
+  return std::fabs(a - b) / u;
+}
+
+template <class L>
+bool bgk(double (&f)[L::Q], const fx::Consts& k) {
+  fx::i64 rq, jq[3];
+  return fx::fluid_collide<L, false>(f, k, rq, jq);
+}
+
+template <class L>
+bool smagorinsky(double (&f)[L::Q], const fx::Consts& k) {
+  fx::i64 rq, jq[3];
+  return fx::fluid_collide<L, true>(f, k, rq, jq);
+}
+
+int fails = 0;
+#define CHECK(c, ...)                  \
+  do {                                 \
+    if (!(c)) {                        \
+      std::printf("FAIL: " __VA_ARGS__); \
+      std::printf("\n");               \
+      ++fails;                         \
+    }                                  \
+  } while (0)
+
+template <class L>
+void run(bool smag, int n, unsigned seed) {
+  constexpr int Q = L::Q;
+  std::mt19937_64 rng(seed);
+  std::uniform_real_distribution<double> U(-1.0, 1.0);
+  const double omega = 1.9725868, cs = 0.1;
+  const double nu = (1.0 / omega - 0.5) / 3.0;
+  fx::Consts k;
+  fx::fill_consts(k, omega, smag ? cs : 0.0, nu);
+  double worst = 0;
+  long not_nearest = 0, total = 0;
+  for (int c = 0; c < n; ++c) {
+    const LD rho = 1.0L + 0.2L * U(rng);
+    const LD u[3] = {0.1L * U(rng), 0.1L * U(rng), 0.1L * U(rng)};
+    const LD usq = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+    double f[Q], want[Q];
+    for (int i = 0; i < Q; ++i) {
+      const LD cu = 3 * (L::ex(i) * u[0] + L::ey(i) * u[1] + L::ez(i) * u[2]);
+      const LD feq = w_of<L>(i) * rho * (1 + cu + 0.5L * cu * cu - 1.5L * usq);
+      f[i] = static_cast<double>(feq * (1 + 2e-3L * U(rng)));
+    }
+    collide_exact<L>(f, smag, omega, cs, want);
+    const bool ok = smag ? smagorinsky<L>(f, k) : bgk<L>(f, k);
+    CHECK(ok, "D3Q%d cell %d outside the fixed-point ranges", Q, c);
+    if (!ok) continue;
+    for (int i = 0; i < Q; ++i) {
+      const double e = ulps(f[i], want[i]);
+      worst = e > worst ? e : worst;
+      not_nearest += e != 0;
+      ++total;
+    }
+  }
+  std::printf("D3Q%d %s: %d cells, largest difference %.3g ulp, %.3g %% not the nearest double\n",
+              Q, smag ? "Smagorinsky" : "BGK", n, worst, 100.0 * not_nearest / total);
+  CHECK(worst <= 3.0, "D3Q%d %s: %.3g ulp", Q, smag ? "smag" : "bgk", worst);
+}
+
+void conversions(unsigned seed) {
+  std::mt19937_64 rng(seed);
+  std::uniform_real_distribution<double> U(-1.0, 1.0);
+  // doubles with at most 62 fractional bits convert exactly and back
+  for (int t = 0; t < 1000000; ++t) {
+    const double d = std::ldexp(U(rng), -static_cast<int>(rng() % 11));
+    if (std::fabs(d) < 0x1p-10) continue;
+    const double back = fx::to_f64(fx::from_f64(d));
+    CHECK(back == d, "round trip %.17g -> %.17g", d, back);
+    if (fails > 10) return;
+  }
+  // to_f64 rounds to nearest: compare with long double
+  for (int t = 0; t < 1000000; ++t) {
+    const fx::i64 v = static_cast<fx::i64>(rng()) >> (1 + rng() % 62);
+    const double want = static_cast<double>(std::ldexp(static_cast<LD>(v), -62));
+    CHECK(fx::to_f64(v) == want, "to_f64(%lld)", v);
+    if (fails > 10) return;
+  }
+  CHECK(fx::from_f64(0.0) == 0 && fx::from_f64(-0.0) == 0 && fx::from_f64(1e-300) == 0, "zero");
+  CHECK(fx::from_f64(1.5) == (static_cast<fx::i64>(3) << 61), "1.5");
+  CHECK(fx::from_f64(-1.0) == -(static_cast<fx::i64>(1) << 62), "-1");
+  // 1/(2 rho) to 2^-59 over the accepted density range
+  for (int t = 0; t < 200000; ++t) {
+    const fx::i64 rq = static_cast<fx::i64>(std::ldexp(1.25 + 0.75 * U(rng), 59));
+    const LD r = std::ldexp(static_cast<LD>(fx::recip2_q63(rq)), -63);
+    const LD want = 1 / (2 * std::ldexp(static_cast<LD>(rq), -59));
+    CHECK(std::fabs(r - want) <= 0x1p-58L, "recip2 %lld", rq);
+    if (fails > 10) return;
+  }
+  std::printf("conversions: checked\n");
+}
+
+template <class L>
+void guards() {
+  constexpr int Q = L::Q;
+  fx::Consts k;
+  fx::fill_consts(k, 1.5, 0.0, (1.0 / 1.5 - 0.5) / 3.0);
+  double f[Q];
+  for (int i = 0; i < Q; ++i) f[i] = static_cast<double>(L::wlit(i));
+  f[0] = 0.5;  // a population at the limit
+  CHECK(!bgk<L>(f, k) && f[0] == 0.5, "guard |f| < 1/2");
+  for (int i = 0; i < Q; ++i) f[i] = 0.3 * static_cast<double>(L::wlit(i));  // rho = 0.3
+  CHECK(!bgk<L>(f, k), "guard rho >= 1/2");
+  for (int i = 0; i < Q; ++i) f[i] = static_cast<double>(L::wlit(i));
+  f[1] = NAN;
+  CHECK(!bgk<L>(f, k), "guard NaN");
+  for (int i = 0; i < Q; ++i) f[i] = static_cast<double>(L::wlit(i));
+  f[1] += 0.3;  // speed 1 has ex = +1: jx = 0.3
+  CHECK(!bgk<L>(f, k), "guard |j| < 1/4");
+  for (int i = 0; i < Q; ++i) f[i] = static_cast<double>(L::wlit(i));
+  CHECK(bgk<L>(f, k), "state at rest accepted");
+}
+
+int main(int argc, char** argv) {
+  const int q = argc > 1 ? std::atoi(argv[1]) : 19;
+  const bool smag = argc > 2 && std::atoi(argv[2]) != 0;
+  const int n = argc > 3 ? std::atoi(argv[3]) : 20000;
+  const unsigned seed = argc > 4 ? static_cast<unsigned>(std::atoi(argv[4])) : 1u;
+  if (q == 0) {
+    conversions(seed);
+    guards<Lattice<15>>();
+    guards<Lattice<19>>();
+    guards<Lattice<27>>();
+  } else if (q == 15) {
+    run<Lattice<15>>(smag, n, seed);
+  } else if (q == 19) {
+    run<Lattice<19>>(smag, n, seed);
+  } else {
+    run<Lattice<27>>(smag, n, seed);
+  }
+  return fails ? 1 : 0;
+}

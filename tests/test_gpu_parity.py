@@ -78,7 +78,11 @@ def test_tlbmexec_cli_fp32_bit_exact(tmp_path):
         assert got[f] == h, f
 
 
-def fast_vs_reference(name, prec, tmp_path, steps=None):
+# the two fast FP64 paths: fluid nodes in exact fixed point (the default) or on the FP64 pipe
+FAST64 = ["fast", "fast-fp64"]
+
+
+def fast_vs_reference(name, prec, tmp_path, steps=None, arith="fast"):
     spec = CASES[name]["spec"]
     d_ref = os.path.join(str(tmp_path), "ref")
     d_fast = os.path.join(str(tmp_path), "fast")
@@ -86,7 +90,7 @@ def fast_vs_reference(name, prec, tmp_path, steps=None):
     write_case_inputs(name, d_fast)
     steps = steps or spec["num_ts"]
     out = []
-    for d, p, a in ((d_ref, "f64", "reference"), (d_fast, prec, "fast")):
+    for d, p, a in ((d_ref, "f64", "reference"), (d_fast, prec, arith)):
         part = T.TLBMPartition(d, precision=p, arithmetic=a)
         part.run(0, steps)
         out.append(part.macros())
@@ -94,20 +98,23 @@ def fast_vs_reference(name, prec, tmp_path, steps=None):
     return out
 
 
-def test_fast_fp64_channel32_2000_within_1e12(tmp_path):
-    ref, fast = fast_vs_reference("channel32_q19_2000", "f64", tmp_path)
-    for fn, a, b in zip(("ux", "uy", "uz", "rho"), fast, ref):
-        err = rel_inf(a, b)
-        assert err <= 1e-12, (fn, err)
+@pytest.mark.parametrize("arith", FAST64)
+def test_fast_fp64_channel32_2000_within_1e12(arith, tmp_path):
+    ref, fast = fast_vs_reference("channel32_q19_2000", "f64", tmp_path, arith=arith)
+    errs = [rel_inf(a, b) for a, b in zip(fast, ref)]
+    print("channel 32x32x128, 2000 steps, %s: rel_inf ux %.2e uy %.2e uz %.2e rho %.2e"
+          % (arith, *errs))
+    assert max(errs) <= 1e-12, errs
 
 
+@pytest.mark.parametrize("arith", FAST64)
 @pytest.mark.parametrize("name,steps", [("q19_sphere_smag", 150), ("q27_sphere_smag", 150),
                                         ("q15_sphere_smag", 150), ("q19_periodic_bgk", None),
                                         ("q27_sphere_bgk", None)])
-def test_fast_fp64_small_within_1e12(name, steps, tmp_path):
+def test_fast_fp64_small_within_1e12(name, steps, arith, tmp_path):
     """The Re=200 Smagorinsky cases amplify round-off differences between two FP64 evaluation
     orders (about 2e-12 after 300 steps), so they are compared after 150 steps."""
-    ref, fast = fast_vs_reference(name, "f64", tmp_path, steps=steps)
+    ref, fast = fast_vs_reference(name, "f64", tmp_path, steps=steps, arith=arith)
     for fn, a, b in zip(("ux", "uy", "uz", "rho"), fast, ref):
         assert rel_inf(a, b) <= 1e-12, fn
 
@@ -125,8 +132,9 @@ def sphere_pack_slab(q, nx=128, ny=64, nz=64, seed=2024):
 PACK_STEPS = {19: 200, 27: 200}
 
 
+@pytest.mark.parametrize("arith", FAST64)
 @pytest.mark.parametrize("q", [19, 27])
-def test_fast_fp64_sphere_pack_within_1e12(q):
+def test_fast_fp64_sphere_pack_within_1e12(q, arith):
     """The bench's form (fast FP64, BGK + Smagorinsky) on the bench's kind of geometry against
     the reference-arithmetic kernel, whose files are byte-identical to the reference's.  At
     Re = 200 the flow through the pack is unsteady and amplifies any round-off difference
@@ -134,43 +142,75 @@ def test_fast_fp64_sphere_pack_within_1e12(q):
     count that holds 1e-12 (PACK_STEPS); the error at that point is printed."""
     g, p = sphere_pack_slab(q)
     out = []
-    for arith in ("reference", "fast"):
+    for a in ("reference", arith):
         part = T.TLBMPartition.from_arrays(T.problem_from_params(p), g.nd_type, precision="f64",
-                                           arithmetic=arith)
+                                           arithmetic=a)
         part.run(0, PACK_STEPS[q])
         out.append(part.macros())
         part.close()
     ref, fast = out
     errs = [rel_inf(a, b) for a, b in zip(fast, ref)]
-    print("D3Q%d sphere pack, %d steps: rel_inf ux %.2e uy %.2e uz %.2e rho %.2e"
-          % (q, PACK_STEPS[q], *errs))
+    print("D3Q%d sphere pack, %d steps, %s: rel_inf ux %.2e uy %.2e uz %.2e rho %.2e"
+          % (q, PACK_STEPS[q], arith, *errs))
     assert all(np.all(np.isfinite(a)) for a in fast)
     assert max(errs) <= 1e-12, errs
 
 
+@pytest.mark.parametrize("arith", FAST64)
 @pytest.mark.parametrize("name", ["q19_cavity_lid", "q27_cavity_lid"])
-@pytest.mark.parametrize("steps", [12, 200])
-def test_fast_fp64_moving_wall_within_1e12(name, steps, tmp_path):
+def test_fast_fp64_moving_wall_within_1e12(name, arith, tmp_path):
     """Node type 5 (set_uz_bc, include/LatticeStructure.hpp:167-177, with its uy[spd] read) in
-    fast arithmetic against the reference-arithmetic kernel on the lid-driven cavity fixtures:
-    the golden run's 12 steps and a longer 200-step run."""
-    ref, fast = fast_vs_reference(name, "f64", tmp_path, steps=steps)
+    fast arithmetic against the reference-arithmetic kernel on the lid-driven cavity fixtures
+    (the golden run's 12 steps; this 10^3 cavity at omega = 1.947 diverges after about 40 steps
+    in both arithmetics, the reference's included)."""
+    ref, fast = fast_vs_reference(name, "f64", tmp_path, arith=arith)
     errs = [rel_inf(a, b) for a, b in zip(fast, ref)]
-    print("%s fast FP64, %d steps: rel_inf ux %.2e uy %.2e uz %.2e rho %.2e" % (name, steps, *errs))
+    print("%s %s: rel_inf ux %.2e uy %.2e uz %.2e rho %.2e" % (name, arith, *errs))
     assert max(errs) <= 1e-12, errs
 
 
-@pytest.mark.parametrize("prec,tol", [("f32", 1e-4), ("f16", 2e-2), ("bf16", 1e-1),
-                                      ("bf16m", 1e-3)])
-def test_reduced_precision_velocity_error(prec, tol, tmp_path):
+@pytest.mark.parametrize("arith", FAST64)
+@pytest.mark.parametrize("q", [19, 27])
+def test_fast_fp64_moving_wall_couette_within_1e12(q, arith):
+    """A stable moving-wall flow for a long comparison: solid wall at y = 0, type-5 wall at
+    y = ny - 1 moving at u_z = 0.05, periodic in x and z (plane Couette flow, Re 10).  Fast FP64
+    against the reference-arithmetic kernel after 400 steps."""
+    nx, ny, nz = 8, 12, 16
+    types = np.zeros((nz, ny, nx), np.int32)
+    types[:, 0, :] = G.SOLID
+    types[:, -1, :] = 5
+    geom = G.Geometry(nx, ny, nz, types.reshape(-1))
+    p = G.params_lattice_units(geom, "D3Q%d" % q, 0.05, 10.0, float(ny), 400)
+    out = []
+    for a in ("reference", arith):
+        part = T.TLBMPartition.from_arrays(T.problem_from_params(p), geom.nd_type,
+                                           precision="f64", arithmetic=a)
+        part.run(0, 400)
+        out.append(part.macros())
+        part.close()
+    ref, fast = out
+    assert np.abs(ref[2]).max() > 1e-3  # the wall drives a flow
+    errs = [rel_inf(a, b) for a, b in zip(fast, ref)]
+    print("D3Q%d Couette, 400 steps, %s: rel_inf ux %.2e uy %.2e uz %.2e rho %.2e"
+          % (q, arith, *errs))
+    assert all(np.all(np.isfinite(a)) for a in fast)
+    assert max(errs) <= 1e-12, errs
+
+
+# velocity bars at about twice the measured errors (GB300): f32 1.28e-5, f16 5.86e-4,
+# bf16 4.30e-3, bf16m 2.79e-4; density bars as before
+@pytest.mark.parametrize("prec,tol,rho_tol", [("f32", 2.6e-5, 1e-3), ("f16", 1.2e-3, 2e-1),
+                                              ("bf16", 9e-3, 1.0), ("bf16m", 6e-4, 1e-2)])
+def test_reduced_precision_velocity_error(prec, tol, rho_tol, tmp_path):
     """Velocity-magnitude relative L2 error against FP64 after 2000 steps of the channel; the
     moment-shifted BF16 storage keeps it within 1e-3."""
     ref, fast = fast_vs_reference("channel32_q19_2000", prec, tmp_path)
     umag = lambda m: np.sqrt(m[0].astype(np.float64) ** 2 + m[1] ** 2 + m[2] ** 2)
     err = rel_l2(umag(fast), umag(ref))
-    print("%s velocity L2 error vs FP64: %.3e" % (prec, err))
+    rho_err = rel_inf(fast[3], ref[3])
+    print("%s velocity L2 error vs FP64: %.3e; density rel_inf %.3e" % (prec, err, rho_err))
     assert err <= tol
-    assert rel_inf(fast[3], ref[3]) <= 10 * tol
+    assert rho_err <= rho_tol
 
 
 def small_problem(q, nx=7, ny=5, nz=6, types=None, cs=0.0, time_avg=0, seed=0):
@@ -425,9 +465,10 @@ def test_async_output_copies_overlap_later_steps():
     b.close()
 
 
+@pytest.mark.parametrize("arith", FAST64)
 @pytest.mark.parametrize("q,dims", [(19, (1, 5, 12)), (19, (6, 1, 12)), (27, (1, 1, 10)),
                                     (15, (2, 3, 9)), (19, (33, 2, 7))])
-def test_fast_wrap_on_degenerate_lattices(q, dims):
+def test_fast_wrap_on_degenerate_lattices(q, dims, arith):
     """Periodic wrap where x - 1 and x + 1 (or y - 1, y + 1) are the cell itself or each other:
     the fast kernel's branch-free wrap against the reference-arithmetic kernel's neighbour
     table, FP64 fast within 1e-12 after 30 steps (fluid, solid, inlet and outlet nodes).
@@ -441,9 +482,9 @@ def test_fast_wrap_on_degenerate_lattices(q, dims):
     geom = G.Geometry(nx, ny, nz, types)
     p = G.params_lattice_units(geom, "D3Q%d" % q, 0.04, 30.0, 3.0, 30, cs=0.1)
     out = []
-    for arith in ("reference", "fast"):
+    for a in ("reference", arith):
         part = T.TLBMPartition.from_arrays(T.problem_from_params(p), types, precision="f64",
-                                           arithmetic=arith)
+                                           arithmetic=a)
         part.run(0, 30)
         out.append(part.macros())
         part.close()
@@ -453,3 +494,32 @@ def test_fast_wrap_on_degenerate_lattices(q, dims):
     for k in range(3):
         assert np.abs(fast[k] - ref[k]).max() <= 1e-12 * u_scale
     assert rel_inf(fast[3], ref[3]) <= 1e-12
+
+
+@pytest.mark.parametrize("q", [15, 19, 27])
+@pytest.mark.parametrize("cs", [0.0, 0.1])
+def test_fixed_point_path_runs_and_falls_back(q, cs):
+    """The fixed-point fluid collision is what runs for FP64 in fast arithmetic: from a smooth
+    non-equilibrium state its populations differ in the last bits from the FP64-pipe path's
+    (and agree to 1e-13).  A state outside its ranges (|j_z| = 0.3 > 1/4 everywhere) is collided
+    by the FP64 code instead: then the two paths agree bit for bit."""
+    g = G.sphere_in_box(16, 12, 20, 3, 8, 6, 10)
+    p = G.params_lattice_units(g, "D3Q%d" % q, 0.05, 40.0, 6.0, 10, cs=cs)
+    n = g.num_nodes
+    z, y, x = np.meshgrid(np.arange(g.nz), np.arange(g.ny), np.arange(g.nx), indexing="ij")
+    for uz, same in ((0.03, False), (0.3, True)):
+        fields = [0.01 * np.sin(2 * np.pi * x / g.nx).reshape(-1),
+                  0.01 * np.cos(2 * np.pi * y / g.ny).reshape(-1), np.full(n, uz),
+                  (1.0 + 0.01 * np.cos(2 * np.pi * z / g.nz)).reshape(-1)]
+        pops = []
+        for arith in FAST64:
+            part = T.TLBMPartition.from_arrays(T.problem_from_params(p), g.nd_type,
+                                               precision="f64", arithmetic=arith)
+            part.load_restart(*fields)
+            part.run(0, 2)
+            pops.append(part.populations(0))
+            part.close()
+        fluid = np.repeat(g.nd_type == G.FLUID, q)
+        a, b = pops[0][fluid], pops[1][fluid]
+        assert np.abs(a - b).max() <= 1e-13
+        assert np.array_equal(a, b) == same, (uz, int((a != b).sum()))

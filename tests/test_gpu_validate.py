@@ -32,10 +32,18 @@ def reference_gold(name):
     return np.sqrt(u[0] ** 2 + u[1] ** 2 + u[2] ** 2)
 
 
+# about twice the measured differences (GB300): q19_sphere_bgk f32 9.05e-6, f16 1.42e-4,
+# bf16 1.07e-3; q27_sphere_smag f32 1.04e-5, f16 1.97e-3, bf16 1.77e-2
+TOL = {("q19_sphere_bgk", "f32"): 2e-5, ("q19_sphere_bgk", "f16"): 3e-4,
+       ("q19_sphere_bgk", "bf16"): 2.2e-3, ("q27_sphere_smag", "f32"): 2.1e-5,
+       ("q27_sphere_smag", "f16"): 4e-3, ("q27_sphere_smag", "bf16"): 3.6e-2}
+
+
 @pytest.mark.parametrize("name", ["q19_sphere_bgk", "q27_sphere_smag"])
-@pytest.mark.parametrize("form,tol", [(("f32", "reference"), 0.0), (("f32", "fast"), 1e-4),
-                                      (("f16", "fast"), 5e-3), (("bf16", "fast"), 2e-2)])
-def test_validate_py_against_reference_gold(name, form, tol, tmp_path):
+@pytest.mark.parametrize("form", [("f32", "reference"), ("f32", "fast"), ("f16", "fast"),
+                                  ("bf16", "fast")])
+def test_validate_py_against_reference_gold(name, form, tmp_path):
+    tol = 0.0 if form[1] == "reference" else TOL[(name, form[0])]
     gold = reference_gold(name)
     write_case_inputs(name, str(tmp_path))
     part = T.TLBMPartition(str(tmp_path), precision=form[0], arithmetic=form[1])

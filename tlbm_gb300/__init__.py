@@ -46,7 +46,7 @@ class Options(ctypes.Structure):
                 ("arithmetic", ctypes.c_int), ("closure", ctypes.c_int),
                 ("block_x", ctypes.c_int), ("block_y", ctypes.c_int), ("device", ctypes.c_int),
                 ("rbgk", ctypes.c_int), ("mrt", ctypes.c_int), ("mrt_ghost_rate", ctypes.c_float),
-                ("reserved", ctypes.c_int * 6)]
+                ("f64_pipe", ctypes.c_int), ("reserved", ctypes.c_int * 5)]
 
 
 class Problem(ctypes.Structure):
@@ -178,6 +178,10 @@ def options(precision="f32", arithmetic=None, block_x=0, block_y=0, device=0,
     o.precision = PREC[precision]
     if arithmetic is None:
         arithmetic = "fast" if precision in ("bf16", "f16", "bf16m") else "reference"
+    if arithmetic == "fast-fp64":
+        # FP64 storage, fast arithmetic with the fluid collision on the FP64 pipe (f64_pipe)
+        arithmetic = "fast"
+        o.f64_pipe = 1
     o.arithmetic = ARITH[arithmetic]
     o.block_x, o.block_y, o.device = block_x, block_y, device
     o.rbgk = int(bool(rbgk))

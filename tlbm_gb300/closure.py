@@ -279,13 +279,19 @@ def calibrate(cl, snaps, cx, cy, cz, u_in, re, noise_amp, calib_step, zp, jet_ra
     return best, scores
 
 
+FLOORS = (0.0, 0.02, 0.03, 0.04, 0.05, 0.06, 0.07, 0.08)
+
+
 def study(cx=128, cy=64, cz=64, factor=4, u_in=0.05, re=3000.0, noise_amp=0.01,
           coarse_steps=1024, snap_every=64, train_from=512, epochs=30, device=0, seed=11,
-          fine_cs=0.05, jet_ratio=0.5, calib_step=None):
-    """The learned-closure experiment; returns errors of Smagorinsky (cs = 0.1), the learned
-    closure, its Smagorinsky floor alone and plain BGK against the filtered fine run at
+          fine_cs=0.05, jet_ratio=0.5, calib_step=None, floors=FLOORS,
+          multipliers=(0.0, 1.0, 3.0, 10.0, 30.0)):
+    """The learned-closure experiment; returns errors against the filtered fine run at
     `coarse_steps` (held out: training uses snapshots before it, calibration the one at
-    `calib_step`), and their costs per step."""
+    `calib_step`) and costs per step of: Smagorinsky at cs = 0.1 (the reference's model at the
+    configured coefficient), Smagorinsky at the cs that scores best on the calibration snapshot
+    over the same grid of floors (the calibrated judge), the learned closure, its Smagorinsky
+    floor alone, and plain BGK."""
     snaps, omega_f = run_fine(cx, cy, cz, factor, u_in, re, noise_amp, coarse_steps, snap_every,
                               device=device, seed=seed, fine_cs=fine_cs, jet_ratio=jet_ratio)
     nu_c = u_in * cy / re
@@ -297,14 +303,18 @@ def study(cx=128, cy=64, cz=64, factor=4, u_in=0.05, re=3000.0, noise_amp=0.01,
     if calib_step is None:
         calib_step = max(k for k in snaps if k < coarse_steps)
     (floor, mult), scores = calibrate(cl, snaps, cx, cy, cz, u_in, re, noise_amp, calib_step,
-                                      zp, jet_ratio, device, seed)
+                                      zp, jet_ratio, device, seed, floors, multipliers)
     cal = dict(cl, out_scale=cl["out_scale"] * mult, floor_cs=floor)
+    # Smagorinsky alone, calibrated on the same snapshot over the same coefficients (k = 0 runs)
+    smag_cs = min((fl for fl in floors if fl > 0), key=lambda fl: scores[(fl, 0.0)])
     out = {"samples": int(len(nut)), "nu_t_mean": float(nut.mean()), "nu": nu_c,
            "fine_finite": bool(np.isfinite(ref).all()),
            "loss_initial": float(cl["loss_initial"]), "loss_final": float(cl["losses"][-1]),
            "calibration": {"step": calib_step, "floor_cs": floor, "multiplier": mult,
+                           "smagorinsky_cs": smag_cs,
                            "scores": {"%g,%g" % k: v for k, v in scores.items()}}}
     for name, kw in (("smagorinsky", {"cs": 0.1}),
+                     ("smagorinsky_calibrated", {"cs": smag_cs}),
                      ("learned", {"closure": cal, "cs": floor}),
                      ("floor_only", {"cs": floor}),
                      ("none", {})):

@@ -176,6 +176,8 @@ Status apply_config_file(const std::string& path, tlbm_options* opt) {
       opt->mrt = std::atoi(val.c_str()) != 0;
     } else if (key == "mrt_ghost_rate") {
       opt->mrt_ghost_rate = static_cast<float>(std::atof(val.c_str()));
+    } else if (key == "f64_pipe") {
+      opt->f64_pipe = std::atoi(val.c_str()) != 0;
     } else {
       return Status::err(TLBM_ERR_INVALID_ARGUMENT, path + ": unknown key " + key);
     }
@@ -449,6 +451,13 @@ Status Engine::init(const int32_t* nd_type, const int32_t* parts, int size) {
   }
   pb_.has_type5 = has_type5_ ? 1 : 0;
   fill_derived(pb_, q_, sb_);
+  // fluid collision in exact fixed point (physics_fx.cuh) for FP64 storage in fast arithmetic;
+  // its rate constants need 0 < omega < 2 (nu > 0)
+  pb_.fx = (store_ == kStoreF64 && !ref_arith_ && !opt_.f64_pipe && prob_.omega > 0.0 &&
+            prob_.omega < 2.0 && prob_.cs >= 0.0)
+               ? 1
+               : 0;
+  if (pb_.fx) fx::fill_consts(pb_.fxk, prob_.omega, prob_.cs, pb_.nu);
 
   const int nb = mass_blocks(pb_);
   TLBM_CUDA(cudaMalloc(&d_partial_, nb * sizeof(double)));

@@ -10,6 +10,7 @@
 #include <cstdint>
 
 #include "lattice.cuh"
+#include "physics_fx.cuh"
 
 namespace tlbm {
 
@@ -38,6 +39,9 @@ struct DevProblem {
   // optional inlet velocity per (x, y) of the z = 0 plane (nx*ny values; null: uniform u_bc)
   const double* inlet_d;
   const float* inlet_f;
+  // FP64 storage, fast arithmetic: fluid nodes collide in exact fixed point (physics_fx.cuh)
+  int fx;
+  fx::Consts fxk;
 };
 
 // whether nodes relax: LBGK, or the regularised BGK of dynamics 2

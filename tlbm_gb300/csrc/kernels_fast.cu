@@ -10,13 +10,13 @@
 namespace tlbm {
 namespace {
 
-template <class L, int K, int kClosure, bool kReg>
+template <class L, int K, int kClosure, bool kReg, bool kFx = false>
 __global__ void __launch_bounds__(128) k_step_fast(StepArgs a) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
   if (x >= a.pb.nx || y >= a.pb.ny) return;
-  cell_step<L, K, kClosure, kReg>(a, x, y, z);
+  cell_step<L, K, kClosure, kReg, true, kFx>(a, x, y, z);
 }
 
 // an opaque copy: the compiler cannot reuse values computed from v before this point
@@ -227,6 +227,12 @@ cudaError_t step_lk(const StepArgs& a, const Launch& l) {
       k_step_fast_mlp<L, K, true><<<g, b, 0, l.stream>>>(a, cl);
     else
       k_step_fast_mlp<L, K, false><<<g, b, 0, l.stream>>>(a, cl);
+  } else if (K == kStoreF64 && a.pb.fx && !a.pb.mcoll) {
+    // FP64 storage: fluid nodes in exact fixed point (physics_fx.cuh)
+    if (a.pb.cs > 0)
+      k_step_fast<L, K, fast::kClosureSmag, false, true><<<g, b, 0, l.stream>>>(a);
+    else
+      k_step_fast<L, K, fast::kClosureNone, false, true><<<g, b, 0, l.stream>>>(a);
   } else if (a.pb.cs > 0 && a.pb.mcoll)
     k_step_fast<L, K, fast::kClosureSmag, true><<<g, b, 0, l.stream>>>(a);
   else if (a.pb.cs > 0)

@@ -217,10 +217,32 @@ __device__ __forceinline__ void accumulate_avg(const StepArgs& a, int c, C rho, 
   avg[3][c] += rho;
 }
 
+// FP64 storage: the fluid collision in exact fixed point (physics_fx.cuh).  Returns false, with
+// f unchanged, when the node does not relax or its state is outside the fixed-point ranges.
+template <class L, int kClosure>
+__device__ __forceinline__ bool fluid_collide_fx(const StepArgs& a, double (&f)[L::Q],
+                                                 double& rho, double& ux, double& uy,
+                                                 double& uz) {
+  const DevProblem& pb = a.pb;
+  if (!relaxes(pb)) return false;
+  fx::i64 rq, jq[3];
+  if (!fx::fluid_collide<L, kClosure == fast::kClosureSmag>(f, pb.fxk, rq, jq)) return false;
+  if (a.time_avg) {
+    rho = fx::to_f64_59(rq);
+    const double inv = fast::recip(rho);
+    ux = fx::to_f64_59(jq[0]) * inv;
+    uy = fx::to_f64_59(jq[1]) * inv;
+    uz = fx::to_f64_59(jq[2]) * inv;
+  }
+  return true;
+}
+
 // kClosure: fast::kClosureNone (BGK) or kClosureSmag (the learned closure has its own kernel,
 // kernels_fast.cu: k_step_fast_mlp); kReg: the moment-space collision (RBGK / MRT);
-// kWrapFree: load_raw's branch-free x/y wrap
-template <class L, int K, int kClosure, bool kReg = false, bool kWrapFree = true>
+// kWrapFree: load_raw's branch-free x/y wrap; kFx: FP64 storage with the fixed-point fluid
+// collision (the FP64 code remains for nodes outside its ranges and for boundary nodes)
+template <class L, int K, int kClosure, bool kReg = false, bool kWrapFree = true,
+          bool kFx = false>
 __device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z) {
   using S = Store<K>;
   using C = typename S::C;
@@ -233,9 +255,13 @@ __device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z
   if (t == kFluid) {
     C f[L::Q];
     unpack<L, K>(raw, f);
-    fast::fluid_collide<L, C, kClosure, kReg>(f, Par<C>::omega(pb), Par<C>::cs(pb),
-                                              Par<C>::nu(pb), Par<C>::ghost_omega(pb),
-                                              relaxes(pb), rho, ux, uy, uz);
+    bool done = false;
+    if constexpr (kFx && K == kStoreF64 && !kReg)
+      done = fluid_collide_fx<L, kClosure>(a, f, rho, ux, uy, uz);
+    if (!done)
+      fast::fluid_collide<L, C, kClosure, kReg>(f, Par<C>::omega(pb), Par<C>::cs(pb),
+                                                Par<C>::nu(pb), Par<C>::ghost_omega(pb),
+                                                relaxes(pb), rho, ux, uy, uz);
     store_cell<L, K>(a, c, f);
   } else {
     boundary_node<L, K, kClosure == fast::kClosureSmag, kReg>(a, x, y, c, t, raw, rho, ux, uy,

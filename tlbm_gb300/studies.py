@@ -22,6 +22,7 @@ from . import geometry as G
 FORMS = {
     "f64-reference": ("f64", "reference"),
     "f64-fast": ("f64", "fast"),
+    "f64-fast-fp64": ("f64", "fast-fp64"),
     "f32": ("f32", "fast"),
     "f16": ("f16", "fast"),
     "bf16": ("bf16", "fast"),
