@@ -2,7 +2,7 @@
 //
 //   fx_harness Q SMAG N SEED
 //
-// For N random near-equilibrium cells (rho in [0.8, 1.2], |u_a| <= 0.1, non-equilibrium parts up
+// For N random near-equilibrium cells (rho in [0.6, 1.6], |u_a| <= 0.2, non-equilibrium parts up
 // to 2e-3 w_i) it collides each cell with fx::fluid_collide and with a long-double evaluation of
 // the reference's formulas (include/LatticeStructure.hpp:70-163: moments, equilibrium with the
 // reference's weights, Smagorinsky rate, BGK relaxation), and prints the largest difference in
@@ -103,8 +103,8 @@ void run(bool smag, int n, unsigned seed) {
   double worst = 0;
   long not_nearest = 0, total = 0;
   for (int c = 0; c < n; ++c) {
-    const LD rho = 1.0L + 0.2L * U(rng);
-    const LD u[3] = {0.1L * U(rng), 0.1L * U(rng), 0.1L * U(rng)};
+    const LD rho = 1.1L + 0.5L * U(rng);
+    const LD u[3] = {0.2L * U(rng), 0.2L * U(rng), 0.2L * U(rng)};
     const LD usq = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
     double f[Q], want[Q];
     for (int i = 0; i < Q; ++i) {
@@ -167,16 +167,28 @@ void guards() {
   fx::fill_consts(k, 1.5, 0.0, (1.0 / 1.5 - 0.5) / 3.0);
   double f[Q];
   for (int i = 0; i < Q; ++i) f[i] = static_cast<double>(L::wlit(i));
-  f[0] = 0.5;  // a population at the limit
-  CHECK(!bgk<L>(f, k) && f[0] == 0.5, "guard |f| < 1/2");
+  f[0] = 1.0;  // the rest population at its limit
+  CHECK(!bgk<L>(f, k) && f[0] == 1.0, "guard f_0 < 1");
+  for (int i = 0; i < Q; ++i) f[i] = static_cast<double>(L::wlit(i));
+  f[0] = -0.01;
+  CHECK(!bgk<L>(f, k), "guard f_0 >= 0");
+  for (int i = 0; i < Q; ++i) f[i] = static_cast<double>(L::wlit(i));
+  f[1] = 0.5;  // a moving population at its limit
+  CHECK(!bgk<L>(f, k), "guard |f_i| < 1/2");
   for (int i = 0; i < Q; ++i) f[i] = 0.3 * static_cast<double>(L::wlit(i));  // rho = 0.3
   CHECK(!bgk<L>(f, k), "guard rho >= 1/2");
   for (int i = 0; i < Q; ++i) f[i] = static_cast<double>(L::wlit(i));
   f[1] = NAN;
   CHECK(!bgk<L>(f, k), "guard NaN");
   for (int i = 0; i < Q; ++i) f[i] = static_cast<double>(L::wlit(i));
-  f[1] += 0.3;  // speed 1 has ex = +1: jx = 0.3
-  CHECK(!bgk<L>(f, k), "guard |j| < 1/4");
+  f[1] += 0.4;  // speed 1 has ex = +1: jx = 0.4 > 0.234 rho (rho = 1.4)
+  CHECK(!bgk<L>(f, k), "guard |j| < 0.234 rho");
+  for (int i = 0; i < Q; ++i) f[i] = 1.5 * static_cast<double>(L::wlit(i));
+  f[1] += 0.3;  // rho = 1.8, jx = 0.3 < 0.234 rho: accepted
+  CHECK(bgk<L>(f, k), "|j| < 0.234 rho accepted at rho 1.8");
+  for (int i = 0; i < Q; ++i) f[i] = static_cast<double>(L::wlit(i));
+  f[0] = 0.9;  // rho ~ 1.57 with a rest population above 1/2: accepted
+  CHECK(bgk<L>(f, k), "f_0 = 0.9 accepted");
   for (int i = 0; i < Q; ++i) f[i] = static_cast<double>(L::wlit(i));
   CHECK(bgk<L>(f, k), "state at rest accepted");
 }

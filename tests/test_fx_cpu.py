@@ -1,7 +1,7 @@
 """The fixed-point FP64-storage collision (tlbm_gb300/csrc/physics_fx.cuh) compiled for the host:
 random near-equilibrium cells collided by it and by a long-double evaluation of the reference's
 formulas (moments, equilibrium with the reference's weights, Smagorinsky rate, BGK relaxation)
-differ by at most 3 ulp of the result (1 ulp on D3Q19; the 3 ulp are D3Q27's smallest
+differ by at most 3 ulp of the result (2 ulp on D3Q19; the 3 ulp are D3Q27's smallest
 populations, ~0.002, where one ulp is 4e-19), and most results are the nearest double.  The exact
 double <-> fixed-point conversions, the integer reciprocal and the range guards are checked
 too."""
@@ -35,7 +35,7 @@ def test_conversions_reciprocal_and_guards(harness):
 
 
 @pytest.mark.parametrize("smag", [0, 1])
-@pytest.mark.parametrize("q,ulp", [(15, 2), (19, 1), (27, 3)])
+@pytest.mark.parametrize("q,ulp", [(15, 3), (19, 2), (27, 3)])
 def test_collision_within_ulps_of_exact(harness, q, ulp, smag):
     r = subprocess.run([harness, str(q), str(smag), "20000", str(q + smag)], capture_output=True,
                        text=True, timeout=300)

@@ -169,18 +169,23 @@ def test_fast_fp64_moving_wall_within_1e12(name, arith, tmp_path):
     assert max(errs) <= 1e-12, errs
 
 
+def lid_cavity(q, n=12, re=10.0, steps=400):
+    """The reference's LidDrivenCavity layout (python/FluidChannel.py:1179-1219): solid faces
+    xm, xp, ym, zm, zp, the yp face a type-5 lid moving at u_z = 0.05; Re 10 on the cavity
+    size, a rate that keeps the lid's set_uz_bc nudge stable over a long run."""
+    t = np.zeros((n, n, n), np.int32)  # (z, y, x)
+    t[:, :, 0] = t[:, :, -1] = t[:, 0, :] = t[0, :, :] = t[-1, :, :] = G.SOLID
+    t[:, -1, :] = 5
+    geom = G.Geometry(n, n, n, t.reshape(-1))
+    return geom, G.params_lattice_units(geom, "D3Q%d" % q, 0.05, re, float(n), steps)
+
+
 @pytest.mark.parametrize("arith", FAST64)
 @pytest.mark.parametrize("q", [19, 27])
-def test_fast_fp64_moving_wall_couette_within_1e12(q, arith):
-    """A stable moving-wall flow for a long comparison: solid wall at y = 0, type-5 wall at
-    y = ny - 1 moving at u_z = 0.05, periodic in x and z (plane Couette flow, Re 10).  Fast FP64
-    against the reference-arithmetic kernel after 400 steps."""
-    nx, ny, nz = 8, 12, 16
-    types = np.zeros((nz, ny, nx), np.int32)
-    types[:, 0, :] = G.SOLID
-    types[:, -1, :] = 5
-    geom = G.Geometry(nx, ny, nz, types.reshape(-1))
-    p = G.params_lattice_units(geom, "D3Q%d" % q, 0.05, 10.0, float(ny), 400)
+def test_fast_fp64_lid_cavity_long_within_1e12(q, arith):
+    """A stable moving-lid flow for a long comparison: fast FP64 against the reference-arithmetic
+    kernel after 400 steps of a 12^3 lid-driven cavity at Re 10."""
+    geom, p = lid_cavity(q)
     out = []
     for a in ("reference", arith):
         part = T.TLBMPartition.from_arrays(T.problem_from_params(p), geom.nd_type,
@@ -189,11 +194,11 @@ def test_fast_fp64_moving_wall_couette_within_1e12(q, arith):
         out.append(part.macros())
         part.close()
     ref, fast = out
-    assert np.abs(ref[2]).max() > 1e-3  # the wall drives a flow
+    assert all(np.all(np.isfinite(a)) for a in ref)
+    assert np.abs(ref[2]).max() > 1e-3  # the lid drives a flow
     errs = [rel_inf(a, b) for a, b in zip(fast, ref)]
-    print("D3Q%d Couette, 400 steps, %s: rel_inf ux %.2e uy %.2e uz %.2e rho %.2e"
+    print("D3Q%d lid cavity, 400 steps, %s: rel_inf ux %.2e uy %.2e uz %.2e rho %.2e"
           % (q, arith, *errs))
-    assert all(np.all(np.isfinite(a)) for a in fast)
     assert max(errs) <= 1e-12, errs
 
 
@@ -500,14 +505,15 @@ def test_fast_wrap_on_degenerate_lattices(q, dims, arith):
 @pytest.mark.parametrize("cs", [0.0, 0.1])
 def test_fixed_point_path_runs_and_falls_back(q, cs):
     """The fixed-point fluid collision is what runs for FP64 in fast arithmetic: from a smooth
-    non-equilibrium state its populations differ in the last bits from the FP64-pipe path's
-    (and agree to 1e-13).  A state outside its ranges (|j_z| = 0.3 > 1/4 everywhere) is collided
-    by the FP64 code instead: then the two paths agree bit for bit."""
-    g = G.sphere_in_box(16, 12, 20, 3, 8, 6, 10)
+    non-equilibrium state on a periodic box its populations differ in the last bits from the
+    FP64-pipe path's (and agree to 1e-13).  A state outside its ranges (u_z = 0.5 everywhere,
+    above |u| < 0.41) is collided by the FP64 code instead: then the two paths agree bit for
+    bit."""
+    g = G.Geometry(16, 12, 20, np.zeros(16 * 12 * 20, np.int32))  # all fluid, periodic
     p = G.params_lattice_units(g, "D3Q%d" % q, 0.05, 40.0, 6.0, 10, cs=cs)
     n = g.num_nodes
     z, y, x = np.meshgrid(np.arange(g.nz), np.arange(g.ny), np.arange(g.nx), indexing="ij")
-    for uz, same in ((0.03, False), (0.3, True)):
+    for uz, same in ((0.03, False), (0.5, True)):
         fields = [0.01 * np.sin(2 * np.pi * x / g.nx).reshape(-1),
                   0.01 * np.cos(2 * np.pi * y / g.ny).reshape(-1), np.full(n, uz),
                   (1.0 + 0.01 * np.cos(2 * np.pi * z / g.nz)).reshape(-1)]

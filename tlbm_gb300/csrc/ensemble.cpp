@@ -110,6 +110,12 @@ Status Ensemble::init(int n, const tlbm_problem* probs, const int32_t* const* nd
     pb.dynamics = p.dynamics;
     pb.has_type5 = 0;
     fill_derived(pb, q, sb_);
+    // FP64 channels collide fluid nodes in exact fixed point, as a single-lattice handle does
+    pb.fx = (store_ == kStoreF64 && !opt_.f64_pipe && p.omega > 0.0 && p.omega < 2.0 &&
+             p.cs >= 0.0)
+                ? 1
+                : 0;
+    if (pb.fx) fx::fill_consts(pb.fxk, p.omega, p.cs, pb.nu);
     c.div_nx = make_fast_div(static_cast<uint32_t>(p.nx));
     off_type[k] = total;
     total += align(static_cast<size_t>(cells));

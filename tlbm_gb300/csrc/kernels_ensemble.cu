@@ -33,14 +33,14 @@ __global__ void __launch_bounds__(256) k_ensemble_step(EnsembleArgs a) {
       const int x = r - y * s.pb.nx;
       if (ch.q == 19) {
         if (s.pb.cs > 0)
-          cell_step<Lattice<19>, K, fast::kClosureSmag, false, true>(s, x, y, tile.z);
+          cell_step<Lattice<19>, K, fast::kClosureSmag, false, true, K == kStoreF64>(s, x, y, tile.z);
         else
-          cell_step<Lattice<19>, K, fast::kClosureNone, false, true>(s, x, y, tile.z);
+          cell_step<Lattice<19>, K, fast::kClosureNone, false, true, K == kStoreF64>(s, x, y, tile.z);
       } else {
         if (s.pb.cs > 0)
-          cell_step<Lattice<15>, K, fast::kClosureSmag, false, true>(s, x, y, tile.z);
+          cell_step<Lattice<15>, K, fast::kClosureSmag, false, true, K == kStoreF64>(s, x, y, tile.z);
         else
-          cell_step<Lattice<15>, K, fast::kClosureNone, false, true>(s, x, y, tile.z);
+          cell_step<Lattice<15>, K, fast::kClosureNone, false, true, K == kStoreF64>(s, x, y, tile.z);
       }
     }
   }

@@ -224,7 +224,7 @@ __device__ __forceinline__ bool fluid_collide_fx(const StepArgs& a, double (&f)[
                                                  double& rho, double& ux, double& uy,
                                                  double& uz) {
   const DevProblem& pb = a.pb;
-  if (!relaxes(pb)) return false;
+  if (!pb.fx || !relaxes(pb)) return false;
   fx::i64 rq, jq[3];
   if (!fx::fluid_collide<L, kClosure == fast::kClosureSmag>(f, pb.fxk, rq, jq)) return false;
   if (a.time_avg) {
