@@ -10,8 +10,18 @@
 namespace tlbm {
 namespace {
 
+// (a __grid_constant__ parameter: the out-of-line cold path of the fixed-point kernel takes it by
+// reference without a per-thread copy).  The fixed-point kernel is bound by integer issue and
+// dependent-latency stalls: more resident warps per SM hide more of the latency.
+#ifndef TLBM_FX_MIN_BLOCKS
+#define TLBM_FX_MIN_BLOCKS 5
+#endif
+// resident blocks of 128 threads asked of the fixed-point kernel (D3Q27 holds more state: more
+// blocks would spill)
+template <class L>
+constexpr int kFxMinBlocks = L::Q == 27 ? 4 : TLBM_FX_MIN_BLOCKS;
 template <class L, int K, int kClosure, bool kReg, bool kFx = false>
-__global__ void __launch_bounds__(128) k_step_fast(StepArgs a) {
+__global__ void __launch_bounds__(128, kFx ? kFxMinBlocks<L> : 1) k_step_fast(const __grid_constant__ StepArgs a) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;

@@ -217,57 +217,78 @@ __device__ __forceinline__ void accumulate_avg(const StepArgs& a, int c, C rho, 
   avg[3][c] += rho;
 }
 
-// FP64 storage: the fluid collision in exact fixed point (physics_fx.cuh).  Returns false, with
-// f unchanged, when the node does not relax or its state is outside the fixed-point ranges.
-template <class L, int kClosure>
-__device__ __forceinline__ bool fluid_collide_fx(const StepArgs& a, double (&f)[L::Q],
-                                                 double& rho, double& ux, double& uy,
-                                                 double& uz) {
-  const DevProblem& pb = a.pb;
-  if (!pb.fx || !relaxes(pb)) return false;
-  fx::i64 rq, jq[3];
-  if (!fx::fluid_collide<L, kClosure == fast::kClosureSmag>(f, pb.fxk, rq, jq)) return false;
-  if (a.time_avg) {
-    rho = fx::to_f64_59(rq);
-    const double inv = fast::recip(rho);
-    ux = fx::to_f64_59(jq[0]) * inv;
-    uy = fx::to_f64_59(jq[1]) * inv;
-    uz = fx::to_f64_59(jq[2]) * inv;
-  }
-  return true;
-}
-
 // kClosure: fast::kClosureNone (BGK) or kClosureSmag (the learned closure has its own kernel,
 // kernels_fast.cu: k_step_fast_mlp); kReg: the moment-space collision (RBGK / MRT);
 // kWrapFree: load_raw's branch-free x/y wrap; kFx: FP64 storage with the fixed-point fluid
 // collision (the FP64 code remains for nodes outside its ranges and for boundary nodes)
 template <class L, int K, int kClosure, bool kReg = false, bool kWrapFree = true,
           bool kFx = false>
+__device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z);
+
+// FP64 storage, the FP64 code for one cell, out of line: the fixed-point kernel sends here the
+// nodes its hot path does not take (boundary nodes, fluid nodes outside the fixed-point ranges,
+// runs that accumulate time averages), which reload their populations.
+template <class L, int kClosure>
+__device__ __noinline__ void cell_step_f64_cold(const StepArgs& a, int x, int y, int z) {
+  cell_step<L, kStoreF64, kClosure, false, true, false>(a, x, y, z);
+}
+
+// FP64 storage with the fluid collision in exact fixed point (physics_fx.cuh): solid nodes swap
+// and fluid nodes collide here; everything else goes to cell_step_f64_cold.  The hot path holds
+// no FP64 arithmetic, so it stays small for the instruction cache.
+template <class L, int kClosure>
+__device__ __forceinline__ void cell_step_fx(const StepArgs& a, int x, int y, int z) {
+  const DevProblem& pb = a.pb;
+  const int c = x + y * pb.nx + z * pb.nxy;
+  double f[L::Q];
+  load_raw<L, kStoreF64, true>(a, x, y, z, c, f);
+  const uint8_t t = pb.nd_type[c];
+  if (!a.time_avg && pb.fx) {
+    double* __restrict__ dst = static_cast<double*>(a.dst);
+    const size_t n = static_cast<size_t>(pb.n);
+    if (t == kSolid) {
+#pragma unroll
+      for (int i = 0; i < L::Q; ++i) dst[i * n + c] = f[L::bb(i)];
+      return;
+    }
+    fx::i64 rq, jq[3];
+    if (t == kFluid && relaxes(pb) &&
+        fx::fluid_collide<L, kClosure == fast::kClosureSmag>(f, pb.fxk, rq, jq)) {
+#pragma unroll
+      for (int i = 0; i < L::Q; ++i) dst[i * n + c] = f[i];
+      return;
+    }
+  }
+  cell_step_f64_cold<L, kClosure>(a, x, y, z);
+}
+
+template <class L, int K, int kClosure, bool kReg, bool kWrapFree, bool kFx>
 __device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z) {
   using S = Store<K>;
   using C = typename S::C;
-  const DevProblem& pb = a.pb;
-  const int c = x + y * pb.nx + z * pb.nxy;
-  typename S::T raw[L::Q];
-  load_raw<L, K, kWrapFree>(a, x, y, z, c, raw);
-  const uint8_t t = pb.nd_type[c];
-  C rho = 0, ux = 0, uy = 0, uz = 0;
-  if (t == kFluid) {
-    C f[L::Q];
-    unpack<L, K>(raw, f);
-    bool done = false;
-    if constexpr (kFx && K == kStoreF64 && !kReg)
-      done = fluid_collide_fx<L, kClosure>(a, f, rho, ux, uy, uz);
-    if (!done)
+  if constexpr (kFx && K == kStoreF64 && !kReg) {
+    cell_step_fx<L, kClosure>(a, x, y, z);
+    return;
+  } else {
+    const DevProblem& pb = a.pb;
+    const int c = x + y * pb.nx + z * pb.nxy;
+    typename S::T raw[L::Q];
+    load_raw<L, K, kWrapFree>(a, x, y, z, c, raw);
+    const uint8_t t = pb.nd_type[c];
+    C rho = 0, ux = 0, uy = 0, uz = 0;
+    if (t == kFluid) {
+      C f[L::Q];
+      unpack<L, K>(raw, f);
       fast::fluid_collide<L, C, kClosure, kReg>(f, Par<C>::omega(pb), Par<C>::cs(pb),
                                                 Par<C>::nu(pb), Par<C>::ghost_omega(pb),
                                                 relaxes(pb), rho, ux, uy, uz);
-    store_cell<L, K>(a, c, f);
-  } else {
-    boundary_node<L, K, kClosure == fast::kClosureSmag, kReg>(a, x, y, c, t, raw, rho, ux, uy,
-                                                              uz);
+      store_cell<L, K>(a, c, f);
+    } else {
+      boundary_node<L, K, kClosure == fast::kClosureSmag, kReg>(a, x, y, c, t, raw, rho, ux,
+                                                                uy, uz);
+    }
+    if (a.time_avg) accumulate_avg<C>(a, c, rho, ux, uy, uz);
   }
-  if (a.time_avg) accumulate_avg<C>(a, c, rho, ux, uy, uz);
 }
 
 }  // namespace tlbm
