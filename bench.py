@@ -211,6 +211,34 @@ def cell_bytes(q, precision):
     return 2 * q * sb + 1 + (32 if precision == "bf16m" else 0)
 
 
+def fp64_pipe_peak(device):
+    """DFMA per second of this GPU (the FP64 pipe, which also executes the int64 <-> double
+    conversions), measured by the microbenchmark in tlbm_gb300/csrc/peaks.cu; None if it fails."""
+    import ctypes
+
+    from tlbm_gb300 import build as B
+
+    try:
+        lib = ctypes.CDLL(B.PEAKS_LIB)
+    except OSError:
+        return None
+    out = (ctypes.c_double * 2)()
+    if lib.tlbm_peaks_fp64(ctypes.c_int(device), out) != 0:
+        return None
+    return {"dfma_per_s": float(out[0]), "i2d_per_s": float(out[1])}
+
+
+def pipe_ops_per_cell(lattice, precision, arithmetic):
+    """FP64-pipe thread instructions per cell-update of the step kernel (ncu
+    sm__inst_executed_pipe_fp64 x 32 / cells, from the committed summary), if measured."""
+    path = os.path.join(HERE, "profiles", "traffic.json")
+    if not os.path.exists(path):
+        return None
+    d = json.load(open(path))
+    v = d.get("%s_%s_%s" % (lattice, precision, arithmetic))
+    return None if v is None else v.get("fp64_pipe_ops_per_cell")
+
+
 def traffic_per_cell(lattice, precision):
     """DRAM bytes per cell-update of the step kernel from the committed ncu summary, if any."""
     path = os.path.join(HERE, "profiles", "traffic.json")
@@ -291,6 +319,8 @@ def run_ours(args, dist):
     peak, peak_kind = peaks()
     achieved = n * bytes_per_cell / step_s / 1e9
     tpc = traffic_per_cell(args.lattice, args.precision)
+    pipe = fp64_pipe_peak(dist.local) if args.precision == "f64" else None
+    ops = pipe_ops_per_cell(args.lattice, args.precision, args.arithmetic)
     out = {
         "metric": METRIC,
         "value": round(value, 2),
@@ -334,6 +364,14 @@ def run_ours(args, dist):
         "clocks": clock,
         "final_mass": mass,
     }
+    if pipe is not None:
+        # the FP64 pipe (FMA, conversions): its measured rate and this kernel's use of it
+        fp = {"unit": "op/s", "peak": pipe["dfma_per_s"], "peak_kind": "measured (peaks.cu)",
+              "ops_per_cell": ops}
+        if ops is not None:
+            fp["achieved"] = ops * n / step_s
+            fp["frac"] = round(fp["achieved"] / pipe["dfma_per_s"], 4)
+        out["roofline"]["fp64_pipe"] = fp
     if not args.no_extras:
         out["e2e"] = e2e(args, g, p, dist)
         if dist.rank == 0 and dist.world == 1:
@@ -520,8 +558,10 @@ def e2e(args, g, p, dist, plot_every=100):
 
 
 def run_reference(args, dist):
-    """The reference's CPU timestep (its C restatement in oracle/; the reference's own build
-    needs the reference sources, which are not available at run time) on all host cores."""
+    """The reference's CPU timestep on all host cores: its C restatement in oracle/, pinned
+    byte-identical to the reference's own build.  That build (oracle/_ref, compiled from the
+    reference's sources where they exist) is built for the machine that compiled it; a machine
+    of another architecture without those sources can neither run nor rebuild it."""
     g, p = workload(args)
     sys.path.insert(0, os.path.join(HERE, "tests"))
     import oracle_lib

@@ -132,17 +132,40 @@ def test_inlet_profile_sets_inlet_velocity():
 def test_closure_pipeline_small():
     """A miniature run of the whole pipeline (fine 64x32x32 -> coarse 32x16x16): the network
     trains on the GPU, the learned closure runs fused in collide, and its errors against the
-    filtered fine run are reported next to Smagorinsky's and plain BGK's."""
+    filtered fine run are reported next to Smagorinsky's and plain BGK's (mechanics only; the
+    comparison is made at the configured size below)."""
     out, cl = CL.study(cx=32, cy=16, cz=16, factor=2, u_in=0.05, re=200.0, coarse_steps=256,
                        snap_every=32, train_from=96, epochs=15)
     print(out)
     assert out["fine_finite"]
     assert out["loss_final"] < out["loss_initial"]
     assert out["learned"]["finite"] and out["smagorinsky"]["finite"]
-    # what the trained network gains over the method without it (plain BGK): a finite run, and
-    # a smaller error where plain BGK survives
+
+
+def test_learned_closure_against_smagorinsky_les():
+    """The closure experiment at its configured size (coarse 128x64x64 LES at Re 3000 against a
+    4x finer run, box-filtered), on the held-out final snapshot:
+      * the learned closure beats the reference's Smagorinsky model at its configured cs = 0.1
+        (the sum of mean-profile and log-spectrum errors);
+      * its network is used and changes the flow: the calibration keeps a non-zero output scale,
+        and the result differs from its Smagorinsky floor alone (a zeroed network would give the
+        floor's numbers exactly);
+      * measured against Smagorinsky calibrated on the same snapshot over the same coefficients
+        (which is also the floor alone here), it stays within 3 % on each error: at this
+        resolution the network adds nothing measurable over a calibrated Smagorinsky (measured
+        on GB300: spectrum 0.0935 vs 0.0919, profile 0.0472 vs 0.0473)."""
+    out, cal = CL.study()
     err = lambda e: e["profile_err"] + e["spectrum_log_err"]
-    assert (not out["none"]["finite"]) or err(out["learned"]) <= err(out["none"])
+    L, F = out["learned"], out["floor_only"]
+    S, SC = out["smagorinsky"], out["smagorinsky_calibrated"]
+    print({k: out[k] for k in ("smagorinsky", "smagorinsky_calibrated", "learned", "floor_only")})
+    print(out["calibration"]["floor_cs"], out["calibration"]["multiplier"])
+    assert all(e["finite"] for e in (L, F, S, SC))
+    assert err(L) < 0.6 * err(S)
+    assert out["calibration"]["multiplier"] > 0
+    assert (L["profile_err"], L["spectrum_log_err"]) != (F["profile_err"], F["spectrum_log_err"])
+    assert L["profile_err"] <= 1.03 * SC["profile_err"]
+    assert L["spectrum_log_err"] <= 1.03 * SC["spectrum_log_err"]
 
 
 # lattice weights by |e|^2 (include/D3Q{15,19,27}LatticeStructure.hpp), as the kernels use them

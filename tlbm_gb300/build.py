@@ -24,6 +24,8 @@ BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 BINDIR = os.path.join(HERE, "bin")
 LIB = os.path.join(LIBDIR, "libtlbm_gb300.so")
+# the benchmark's measurement of this GPU's FP64-pipe rate (not part of the engine's C ABI)
+PEAKS_LIB = os.path.join(LIBDIR, "libtlbm_peaks.so")
 EXE = os.path.join(BINDIR, "tLBMexec")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -94,6 +96,13 @@ def build(force: bool = False, verbose: bool = False) -> str:
             list(ex.map(lambda u: _compile(u[0], u[1], verbose), todo))
     if force or todo or _stale(LIB, objs):
         cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", LIB] + objs
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+    peaks_src = os.path.join(CSRC, "peaks.cu")
+    if force or _stale(PEAKS_LIB, [peaks_src]):
+        obj = _compile("peaks.cu", [], verbose)
+        cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", PEAKS_LIB, obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
