@@ -239,13 +239,13 @@ def pipe_ops_per_cell(lattice, precision, arithmetic):
     return None if v is None else v.get("fp64_pipe_ops_per_cell")
 
 
-def traffic_per_cell(lattice, precision):
+def traffic_per_cell(lattice, precision, arithmetic):
     """DRAM bytes per cell-update of the step kernel from the committed ncu summary, if any."""
     path = os.path.join(HERE, "profiles", "traffic.json")
     if not os.path.exists(path):
         return None
     d = json.load(open(path))
-    v = d.get("%s_%s" % (lattice, precision))
+    v = d.get("%s_%s_%s" % (lattice, precision, arithmetic)) or d.get("%s_%s" % (lattice, precision))
     return None if v is None else float(v["dram_bytes_per_cell"])
 
 
@@ -318,7 +318,7 @@ def run_ours(args, dist):
     value = n * args.steps * dist.world / (ms_max / 1e3) / 1e6
     peak, peak_kind = peaks()
     achieved = n * bytes_per_cell / step_s / 1e9
-    tpc = traffic_per_cell(args.lattice, args.precision)
+    tpc = traffic_per_cell(args.lattice, args.precision, args.arithmetic)
     pipe = fp64_pipe_peak(dist.local) if args.precision == "f64" else None
     ops = pipe_ops_per_cell(args.lattice, args.precision, args.arithmetic)
     out = {

@@ -32,11 +32,13 @@ def reference_gold(name):
     return np.sqrt(u[0] ** 2 + u[1] ** 2 + u[2] ** 2)
 
 
-# about twice the measured differences (GB300): q19_sphere_bgk f32 9.05e-6, f16 1.42e-4,
-# bf16 1.07e-3; q27_sphere_smag f32 1.04e-5, f16 1.97e-3, bf16 1.77e-2
+# about twice the measured differences (GB300): q19_sphere_bgk f32 9.05e-6, f16 1.27e-4,
+# bf16 1.20e-3; q27_sphere_smag f32 1.04e-5, f16 1.07e-2, bf16 1.36e-2.  q27_sphere_smag is an
+# unsteady Re-200 flow: its last dump's difference grows with any change of round-off (the f16
+# value moved between 2e-3 and 1.1e-2 with the order of the 16-bit collision's float operations)
 TOL = {("q19_sphere_bgk", "f32"): 2e-5, ("q19_sphere_bgk", "f16"): 3e-4,
-       ("q19_sphere_bgk", "bf16"): 2.2e-3, ("q27_sphere_smag", "f32"): 2.1e-5,
-       ("q27_sphere_smag", "f16"): 4e-3, ("q27_sphere_smag", "bf16"): 3.6e-2}
+       ("q19_sphere_bgk", "bf16"): 2.5e-3, ("q27_sphere_smag", "f32"): 2.1e-5,
+       ("q27_sphere_smag", "f16"): 2.2e-2, ("q27_sphere_smag", "bf16"): 3e-2}
 
 
 @pytest.mark.parametrize("name", ["q19_sphere_bgk", "q27_sphere_smag"])

@@ -10,23 +10,64 @@
 namespace tlbm {
 namespace {
 
-// (a __grid_constant__ parameter: the out-of-line cold path of the fixed-point kernel takes it by
-// reference without a per-thread copy).  The fixed-point kernel is bound by integer issue and
-// dependent-latency stalls: more resident warps per SM hide more of the latency.
-#ifndef TLBM_FX_MIN_BLOCKS
-#define TLBM_FX_MIN_BLOCKS 5
-#endif
-// resident blocks of 128 threads asked of the fixed-point kernel (D3Q27 holds more state: more
-// blocks would spill)
-template <class L>
-constexpr int kFxMinBlocks = L::Q == 27 ? 4 : TLBM_FX_MIN_BLOCKS;
-template <class L, int K, int kClosure, bool kReg, bool kFx = false>
-__global__ void __launch_bounds__(128, kFx ? kFxMinBlocks<L> : 1) k_step_fast(const __grid_constant__ StepArgs a) {
+// (no minimum of resident blocks: stating one, even 1, changes ptxas's register budget, e.g.
+// 64 -> 96 registers for the moment-shifted BF16 step, 15 % slower)
+template <class L, int K, int kClosure, bool kReg>
+__global__ void __launch_bounds__(128) k_step_fast(StepArgs a) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
   if (x >= a.pb.nx || y >= a.pb.ny) return;
-  cell_step<L, K, kClosure, kReg, true, kFx>(a, x, y, z);
+  cell_step<L, K, kClosure, kReg>(a, x, y, z);
+}
+
+// 16-bit storage of f - w (BF16, FP16).  These steps are bound by memory latency (2-byte loads:
+// few bytes in flight per thread), so they state one resident block as their minimum, which
+// leaves ptxas a larger register budget to hoist loads (measured 45.5 against 42.0 GLUPS at
+// the default budget); TLBM_TWO_CELLS_16 gives each thread two cells (step_fast.cuh:
+// cell_step2), a block of (bx, by) threads covering 2 by rows, thread row ty taking rows ty and
+// ty + by of the block's band.
+#ifndef TLBM_TWO_CELLS_16
+#define TLBM_TWO_CELLS_16 1
+#endif
+template <class L, int K, int kClosure>
+__global__ void __launch_bounds__(128, 1) k_step_fast16(StepArgs a) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= a.pb.nx || y >= a.pb.ny) return;
+  cell_step<L, K, kClosure, false>(a, x, y, z);
+}
+
+template <class L, int K, int kClosure, bool kReg>
+__global__ void __launch_bounds__(128, 1) k_step_fast2(StepArgs a) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y0 = blockIdx.y * blockDim.y * 2 + threadIdx.y;
+  const int y1 = y0 + blockDim.y;
+  const int z = blockIdx.z;
+  if (x >= a.pb.nx || y0 >= a.pb.ny) return;
+  cell_step2<L, K, kClosure, kReg>(a, x, y0, y1 < a.pb.ny ? y1 : -1, z);
+}
+
+// FP64 storage with the fluid collision in exact fixed point (step_fast.cuh: cell_step_fx).  The
+// parameter is a __grid_constant__, so the out-of-line FP64 cold path takes it by reference
+// without a per-thread copy.  The kernel is bound by integer issue and dependent-latency stalls:
+// more resident warps per SM hide more of the latency (D3Q27 holds more state: more blocks would
+// spill).
+#ifndef TLBM_FX_MIN_BLOCKS
+#define TLBM_FX_MIN_BLOCKS 5
+#endif
+template <class L>
+constexpr int kFxMinBlocks = L::Q == 27 ? 4 : TLBM_FX_MIN_BLOCKS;
+
+template <class L, int kClosure>
+__global__ void __launch_bounds__(128, kFxMinBlocks<L>)
+    k_step_fast_fx(const __grid_constant__ StepArgs a) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= a.pb.nx || y >= a.pb.ny) return;
+  cell_step_fx<L, kClosure>(a, x, y, z);
 }
 
 // an opaque copy: the compiler cannot reuse values computed from v before this point
@@ -239,10 +280,27 @@ cudaError_t step_lk(const StepArgs& a, const Launch& l) {
       k_step_fast_mlp<L, K, false><<<g, b, 0, l.stream>>>(a, cl);
   } else if (K == kStoreF64 && a.pb.fx && !a.pb.mcoll) {
     // FP64 storage: fluid nodes in exact fixed point (physics_fx.cuh)
-    if (a.pb.cs > 0)
-      k_step_fast<L, K, fast::kClosureSmag, false, true><<<g, b, 0, l.stream>>>(a);
-    else
-      k_step_fast<L, K, fast::kClosureNone, false, true><<<g, b, 0, l.stream>>>(a);
+    if constexpr (K == kStoreF64) {
+      if (a.pb.cs > 0)
+        k_step_fast_fx<L, fast::kClosureSmag><<<g, b, 0, l.stream>>>(a);
+      else
+        k_step_fast_fx<L, fast::kClosureNone><<<g, b, 0, l.stream>>>(a);
+    }
+  } else if ((K == kStoreBF16 || K == kStoreF16) && !a.pb.mcoll) {
+    // 16-bit storage of f - w
+    if constexpr (K == kStoreBF16 || K == kStoreF16) {
+      if (TLBM_TWO_CELLS_16) {
+        const dim3 g2(g.x, (a.pb.ny + 2 * l.by - 1) / (2 * l.by), g.z);
+        if (a.pb.cs > 0)
+          k_step_fast2<L, K, fast::kClosureSmag, false><<<g2, b, 0, l.stream>>>(a);
+        else
+          k_step_fast2<L, K, fast::kClosureNone, false><<<g2, b, 0, l.stream>>>(a);
+      } else if (a.pb.cs > 0) {
+        k_step_fast16<L, K, fast::kClosureSmag><<<g, b, 0, l.stream>>>(a);
+      } else {
+        k_step_fast16<L, K, fast::kClosureNone><<<g, b, 0, l.stream>>>(a);
+      }
+    }
   } else if (a.pb.cs > 0 && a.pb.mcoll)
     k_step_fast<L, K, fast::kClosureSmag, true><<<g, b, 0, l.stream>>>(a);
   else if (a.pb.cs > 0)

@@ -262,33 +262,74 @@ __device__ __forceinline__ void cell_step_fx(const StepArgs& a, int x, int y, in
   cell_step_f64_cold<L, kClosure>(a, x, y, z);
 }
 
-template <class L, int K, int kClosure, bool kReg, bool kWrapFree, bool kFx>
-__device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z) {
+// the part of cell_step after the loads: node-type branch, collision, store
+template <class L, int K, int kClosure, bool kReg>
+__device__ __forceinline__ void cell_compute(const StepArgs& a, int x, int y, int c, uint8_t t,
+                                             const typename Store<K>::T (&raw)[L::Q]) {
   using S = Store<K>;
   using C = typename S::C;
-  if constexpr (kFx && K == kStoreF64 && !kReg) {
-    cell_step_fx<L, kClosure>(a, x, y, z);
-    return;
-  } else {
-    const DevProblem& pb = a.pb;
-    const int c = x + y * pb.nx + z * pb.nxy;
-    typename S::T raw[L::Q];
-    load_raw<L, K, kWrapFree>(a, x, y, z, c, raw);
-    const uint8_t t = pb.nd_type[c];
-    C rho = 0, ux = 0, uy = 0, uz = 0;
-    if (t == kFluid) {
+  const DevProblem& pb = a.pb;
+  C rho = 0, ux = 0, uy = 0, uz = 0;
+  if (t == kFluid) {
+    if constexpr (S::kShifted && !kReg) {
+      // 16-bit storage of f - w: collide the stored shifts themselves
+      float d[L::Q];
+#pragma unroll
+      for (int i = 0; i < L::Q; ++i) d[i] = S::shift_of(raw[i]);
+      fast::fluid_collide_shifted<L, kClosure>(d, Par<C>::omega(pb), Par<C>::cs(pb),
+                                               Par<C>::nu(pb), relaxes(pb), rho, ux, uy, uz);
+      typename S::P* __restrict__ dst = static_cast<typename S::P*>(a.dst);
+      const size_t n = static_cast<size_t>(pb.n);
+#pragma unroll
+      for (int i = 0; i < L::Q; ++i) dst[i * n + c] = S::of_shift(d[i]);
+    } else {
       C f[L::Q];
       unpack<L, K>(raw, f);
       fast::fluid_collide<L, C, kClosure, kReg>(f, Par<C>::omega(pb), Par<C>::cs(pb),
                                                 Par<C>::nu(pb), Par<C>::ghost_omega(pb),
                                                 relaxes(pb), rho, ux, uy, uz);
       store_cell<L, K>(a, c, f);
-    } else {
-      boundary_node<L, K, kClosure == fast::kClosureSmag, kReg>(a, x, y, c, t, raw, rho, ux,
-                                                                uy, uz);
     }
-    if (a.time_avg) accumulate_avg<C>(a, c, rho, ux, uy, uz);
+  } else {
+    boundary_node<L, K, kClosure == fast::kClosureSmag, kReg>(a, x, y, c, t, raw, rho, ux, uy,
+                                                              uz);
   }
+  if (a.time_avg) accumulate_avg<C>(a, c, rho, ux, uy, uz);
+}
+
+template <class L, int K, int kClosure, bool kReg, bool kWrapFree, bool kFx>
+__device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z) {
+  if constexpr (kFx && K == kStoreF64 && !kReg) {
+    cell_step_fx<L, kClosure>(a, x, y, z);
+  } else {
+    const DevProblem& pb = a.pb;
+    const int c = x + y * pb.nx + z * pb.nxy;
+    typename Store<K>::T raw[L::Q];
+    load_raw<L, K, kWrapFree>(a, x, y, z, c, raw);
+    cell_compute<L, K, kClosure, kReg>(a, x, y, c, pb.nd_type[c], raw);
+  }
+}
+
+// Two cells per thread, rows y0 and y1 of one x column: both cells' loads are issued before
+// either is computed, so a thread keeps twice the bytes in flight (the 16-bit kinds move only
+// 2 bytes per load and are otherwise bound by memory latency).  y1 < 0: one cell.
+template <class L, int K, int kClosure, bool kReg>
+__device__ __forceinline__ void cell_step2(const StepArgs& a, int x, int y0, int y1, int z) {
+  const DevProblem& pb = a.pb;
+  const int c0 = x + y0 * pb.nx + z * pb.nxy;
+  typename Store<K>::T r0[L::Q];
+  load_raw<L, K, true>(a, x, y0, z, c0, r0);
+  const uint8_t t0 = pb.nd_type[c0];
+  if (y1 < 0) {
+    cell_compute<L, K, kClosure, kReg>(a, x, y0, c0, t0, r0);
+    return;
+  }
+  const int c1 = x + y1 * pb.nx + z * pb.nxy;
+  typename Store<K>::T r1[L::Q];
+  load_raw<L, K, true>(a, x, y1, z, c1, r1);
+  const uint8_t t1 = pb.nd_type[c1];
+  cell_compute<L, K, kClosure, kReg>(a, x, y0, c0, t0, r0);
+  cell_compute<L, K, kClosure, kReg>(a, x, y1, c1, t1, r1);
 }
 
 }  // namespace tlbm

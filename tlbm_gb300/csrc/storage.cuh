@@ -61,6 +61,9 @@ struct Store<kStoreBF16> {
   static constexpr bool kShifted = true;
   static __device__ __forceinline__ C load(T v, C w) { return w + __bfloat162float(v); }
   static __device__ __forceinline__ T save(C f, C w) { return __float2bfloat16_rn(f - w); }
+  // the stored shift f - w itself
+  static __device__ __forceinline__ C shift_of(T v) { return __bfloat162float(v); }
+  static __device__ __forceinline__ T of_shift(C d) { return __float2bfloat16_rn(d); }
 };
 
 template <>
@@ -72,6 +75,8 @@ struct Store<kStoreF16> {
   static constexpr bool kShifted = true;
   static __device__ __forceinline__ C load(T v, C w) { return w + __half2float(v); }
   static __device__ __forceinline__ T save(C f, C w) { return __float2half_rn(f - w); }
+  static __device__ __forceinline__ C shift_of(T v) { return __half2float(v); }
+  static __device__ __forceinline__ T of_shift(C d) { return __float2half_rn(d); }
 };
 
 template <>
