@@ -111,6 +111,21 @@ def test_ndtype_bad_code(lib, tmp_path):
     assert st == T.ERR_OUT_OF_RANGE and "type 4" in msg
 
 
+def test_ndtype_bad_code_lowest_node_named(lib):
+    """The node types are checked in chunks on several host threads; the error still names the
+    lowest offending node, whichever chunk finds one first."""
+    nx, ny, nz = 256, 128, 128  # 4.19 M nodes: four chunks of 2^20
+    nd = np.zeros(nx * ny * nz, np.int32)
+    nd[3_900_000] = 9
+    nd[2_500_000] = 7
+    nd[1_234_567] = -1
+    st, msg = _create(_problem(nx, ny, nz), nd, precision="f64")
+    assert st == T.ERR_OUT_OF_RANGE and "node 1234567 " in msg and "type -1" in msg
+    nd[1_234_567] = 0
+    st, msg = _create(_problem(nx, ny, nz), nd, precision="f64")
+    assert st == T.ERR_OUT_OF_RANGE and "node 2500000 " in msg and "type 7" in msg
+
+
 def test_parts_beyond_job_size(lib, tmp_path):
     parts = G.partition_1d(8, 8, 12, 3)
     small_inputs(tmp_path, parts=parts)

@@ -273,6 +273,27 @@ def test_time_average_files_match_oracle(tmp_path):
     assert g == c
 
 
+@pytest.mark.parametrize("arith", FAST64)
+def test_fast_fp64_time_averages_within_1e12(arith, tmp_path):
+    """Time averaging on (params.lbm line 15): the fixed-point kernel sends every node of such a
+    run through the FP64 code, which accumulates the averages.  The average files of fast FP64
+    equal the reference arithmetic's within 1e-12 (field-relative) after 30 steps of a box with
+    random fluid, solid, inlet and outlet nodes (Smagorinsky)."""
+    geom, p = small_problem(19, nx=9, ny=7, nz=11, cs=0.1, time_avg=1, seed=5)
+    p.num_ts, p.plot_freq = 30, 10
+    out = {}
+    for a in ("reference", arith):
+        d = str(tmp_path / a)
+        G.write_inputs(d, geom, p)
+        part = T.TLBMPartition(d, precision="f64", arithmetic=a)
+        T.run_like_tlbmexec(part)
+        part.close()
+        out[a] = [np.fromfile(os.path.join(d, f), dtype=np.float64)
+                  for f in ("uAvg.b_dat", "vAvg.b_dat", "wAvg.b_dat", "rhoAvg.b_dat")]
+    for x, y in zip(out[arith], out["reference"]):
+        assert np.all(np.isfinite(x)) and rel_inf(x, y) <= 1e-12, rel_inf(x, y)
+
+
 def test_multi_partition_output_order(tmp_path):
     """A 3-partition parts.lbm (1D z-slabs and a 3D block split) changes only the file order:
     ordering.b_dat and every dump equal the oracle's partition-major files."""

@@ -21,6 +21,7 @@
 #include <cstring>
 #include <fstream>
 #include <sstream>
+#include <thread>
 
 #include "mlp.cuh"
 #include "mlp_kernels.h"
@@ -28,6 +29,27 @@
 #include "trace.h"
 
 namespace tlbm {
+
+namespace {
+
+// Splits [0, n) into contiguous chunks of at least 2^20 items, one per host thread (at most 8),
+// and runs fn(begin, end, &state) on each; states come back in chunk order, so the first chunk
+// that reports something holds the lowest index.
+template <class State, class Fn>
+void for_chunks(int64_t n, std::vector<State>* states, Fn fn) {
+  const int64_t kMinChunk = int64_t{1} << 20;
+  const int64_t hw = std::max(1u, std::thread::hardware_concurrency());
+  const int64_t t = std::max<int64_t>(1, std::min<int64_t>({8, hw, n / kMinChunk}));
+  states->assign(static_cast<size_t>(t), State{});
+  const int64_t per = (n + t - 1) / t;
+  std::vector<std::thread> pool;
+  for (int64_t k = 1; k < t; ++k)
+    pool.emplace_back([&, k] { fn(k * per, std::min(n, (k + 1) * per), &(*states)[k]); });
+  fn(0, std::min(n, per), &(*states)[0]);
+  for (auto& th : pool) th.join();
+}
+
+}  // namespace
 
 // ----------------------------------------------------------------------------- input parsing
 
@@ -319,15 +341,33 @@ Status Engine::init(const int32_t* nd_type, const int32_t* parts, int size) {
   sb_ = store_bytes(store_);
   ob_ = (store_ == kStoreF64) ? 8 : 4;
 
-  // node types: the reference's codes only (python/FluidChannel.py:1386-1397)
+  // node types: the reference's codes only (python/FluidChannel.py:1386-1397); checked and
+  // narrowed to bytes in chunks on several host threads (33.5 M nodes take ~30 ms on one core)
   std::vector<uint8_t> types(static_cast<size_t>(n_));
-  for (int64_t g = 0; g < n_; ++g) {
-    const int32_t t = nd_type[g];
-    if (!(t == 0 || t == 1 || t == 2 || t == 3 || t == 5))
-      return Status::err(TLBM_ERR_OUT_OF_RANGE, "ndType.lbm: node " + std::to_string(g) +
-                                                    " has unknown type " + std::to_string(t));
-    types[g] = static_cast<uint8_t>(t);
-    if (t == 5) has_type5_ = true;
+  {
+    struct Chunk {
+      int64_t bad = -1;
+      bool type5 = false;
+    };
+    std::vector<Chunk> chunks;
+    for_chunks(n_, &chunks, [&](int64_t begin, int64_t end, Chunk* c) {
+      for (int64_t g = begin; g < end; ++g) {
+        const int32_t t = nd_type[g];
+        if (!(t == 0 || t == 1 || t == 2 || t == 3 || t == 5)) {
+          c->bad = g;
+          return;
+        }
+        types[g] = static_cast<uint8_t>(t);
+        c->type5 |= (t == 5);
+      }
+    });
+    for (const Chunk& c : chunks) {
+      if (c.bad >= 0)
+        return Status::err(TLBM_ERR_OUT_OF_RANGE, "ndType.lbm: node " + std::to_string(c.bad) +
+                                                      " has unknown type " +
+                                                      std::to_string(nd_type[c.bad]));
+      has_type5_ |= c.type5;
+    }
   }
 
   // partitions: the reference indexes partSizes[p] with p < size (src/TLBM_Partition.cpp:224)
@@ -832,9 +872,35 @@ Status Engine::copy_outputs_async(void* const host[7]) {
   const size_t bytes = static_cast<size_t>(n_) * ob_;
   const void* dev[7] = {d_macro_[0], d_macro_[1], d_macro_[2], d_macro_[3],
                         d_force_[0], d_force_[1], d_force_[2]};
+  // Page-locked destinations are written by a copy kernel on the copy stream: on GB300 its
+  // stores reach page-locked host memory at the copy engines' rate (~190 GB/s), and some
+  // copy-engine transfers issued from an application process ran at ~16 GB/s.  Other
+  // destinations take cudaMemcpyAsync.
+  const void* ksrc[7];
+  void* kdst[7];
+  int nk = 0;
   for (int k = 0; k < 7; ++k) {
     if (!host[k]) continue;
-    TLBM_CUDA(cudaMemcpyAsync(host[k], dev[k], bytes, cudaMemcpyDeviceToHost, copy_stream_));
+    cudaPointerAttributes at{};
+    const bool pinned = cudaPointerGetAttributes(&at, host[k]) == cudaSuccess &&
+                        at.type == cudaMemoryTypeHost &&
+                        reinterpret_cast<uintptr_t>(host[k]) % 16 == 0 && bytes % 16 == 0;
+    cudaGetLastError();  // a pageable pointer can leave an error state behind
+    if (pinned) {
+      ksrc[nk] = dev[k];
+      kdst[nk] = at.devicePointer ? at.devicePointer : host[k];
+      ++nk;
+    } else {
+      TLBM_CUDA(cudaMemcpyAsync(host[k], dev[k], bytes, cudaMemcpyDeviceToHost, copy_stream_));
+    }
+  }
+  if (nk > 0) {
+    if (sms_ == 0) TLBM_CUDA(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount,
+                                                    opt_.device));
+    Launch cl = launch_;
+    cl.stream = copy_stream_;
+    TLBM_CUDA(launch_copy_words(ksrc, kdst, nk, bytes, 2 * sms_, cl));
+    ++launches_;
   }
   TLBM_CUDA(cudaEventRecord(copies_done_, copy_stream_));
   copies_pending_ = true;

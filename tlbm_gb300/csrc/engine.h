@@ -93,6 +93,7 @@ class Engine {
   std::string workdir_;
   int q_ = 19;
   bool ref_arith_ = true;
+  int sms_ = 0;  // multiprocessors of the device (set on first use)
   int store_ = kStoreF32;
   int sb_ = 4;  // bytes per stored population
   int ob_ = 4;  // bytes per output value

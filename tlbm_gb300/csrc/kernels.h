@@ -82,6 +82,11 @@ int mass_blocks(const DevProblem& pb);
 cudaError_t launch_mass(int q, int store, const DevProblem& pb, const void* f, double* partial,
                         int nblocks, double* out, const Launch& l);
 // out[k] = in[order[k]] for element size `bytes`
+// dst[k][0 .. bytes) = src[k][0 .. bytes) for k < count <= 8, by a kernel (every pointer 16-byte
+// aligned, bytes a multiple of 16; dst may be page-locked host memory, written through the
+// GPU's loads and stores instead of a copy engine); `blocks` CTAs of 256 threads
+cudaError_t launch_copy_words(const void* const* src, void* const* dst, int count, size_t bytes,
+                              int blocks, const Launch& l);
 cudaError_t launch_gather(const void* in, const int32_t* order, int64_t n, int bytes, void* out,
                           const Launch& l);
 

@@ -283,6 +283,39 @@ cudaError_t launch_mass(int q, int store, const DevProblem& pb, const void* f, d
   return by_q_store<Mass>(q, store, pb, f, partial, nblocks, out, l);
 }
 
+struct CopyWords {
+  const uint4* src[8];
+  uint4* dst[8];
+  int count;
+  long long words;
+};
+
+__global__ void __launch_bounds__(256) k_copy_words(const CopyWords c) {
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  const long long i0 = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  for (int k = 0; k < c.count; ++k) {
+    const uint4* __restrict__ s = c.src[k];
+    uint4* __restrict__ d = c.dst[k];
+    for (long long i = i0; i < c.words; i += stride) d[i] = __ldg(s + i);
+  }
+}
+
+cudaError_t launch_copy_words(const void* const* src, void* const* dst, int count, size_t bytes,
+                              int blocks, const Launch& l) {
+  if (count < 0 || count > 8 || bytes % 16 != 0 || blocks < 1) return cudaErrorInvalidValue;
+  CopyWords c{};
+  for (int k = 0; k < count; ++k) {
+    if ((reinterpret_cast<uintptr_t>(src[k]) | reinterpret_cast<uintptr_t>(dst[k])) % 16 != 0)
+      return cudaErrorInvalidValue;
+    c.src[k] = static_cast<const uint4*>(src[k]);
+    c.dst[k] = static_cast<uint4*>(dst[k]);
+  }
+  c.count = count;
+  c.words = static_cast<long long>(bytes / 16);
+  k_copy_words<<<blocks, 256, 0, l.stream>>>(c);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_gather(const void* in, const int32_t* order, int64_t n, int bytes, void* out,
                           const Launch& l) {
   const int b = blocks_for(n);
