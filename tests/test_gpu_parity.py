@@ -522,6 +522,43 @@ def test_fast_wrap_on_degenerate_lattices(q, dims, arith):
     assert rel_inf(fast[3], ref[3]) <= 1e-12
 
 
+def _pairs_case(name, q):
+    """Lattices for the x-pair 16-bit step: the sphere-pack slab (fluid, solid, inlet and
+    outlet planes), the lid cavity (type-5 lid) and periodic boxes of random fluid/solid nodes
+    where x - 2 and x + 2 wrap onto the pair itself (nx = 2) or each other (nx = 4)."""
+    if name == "pack":
+        return sphere_pack_slab(q, nx=64, ny=32, nz=48, seed=7)
+    if name == "cavity":
+        return lid_cavity(q, n=12, steps=60)
+    nx, ny, nz = {"box2": (2, 3, 9), "box4": (4, 1, 12), "box6": (6, 5, 7)}[name]
+    rng = np.random.default_rng(nx * 100 + ny * 10 + q)
+    types = rng.choice([0, 0, 0, 1], size=nx * ny * nz).astype(np.int32)
+    g = G.Geometry(nx, ny, nz, types)
+    return g, G.params_lattice_units(g, "D3Q%d" % q, 0.04, 30.0, 3.0, 60, cs=0.1)
+
+
+@pytest.mark.parametrize("prec", ["bf16", "f16"])
+@pytest.mark.parametrize("q", [15, 19, 27])
+@pytest.mark.parametrize("name", ["pack", "cavity", "box2", "box4", "box6"])
+def test_pair_step_bit_identical_to_one_cell_step(name, q, prec):
+    """16-bit storage on a lattice with nx even runs two cells of a row per thread, each
+    population pair as one 32-bit word; runs with time averaging take the one-cell step.  The
+    populations after 60 steps agree bit for bit, with and without the Smagorinsky rate."""
+    g, p = _pairs_case(name, q)
+    for cs in (0.0, 0.1):
+        pops = []
+        for avg in (1, 0):
+            prob = T.problem_from_params(p)
+            prob.cs = cs
+            prob.time_avg_flag = avg
+            part = T.TLBMPartition.from_arrays(prob, g.nd_type, precision=prec)
+            part.run(0, 60)
+            pops.append(part.populations(0).view(np.uint32))  # f = w + shift, as float32
+            part.close()
+        assert np.array_equal(pops[0], pops[1]), (name, q, prec, cs,
+                                                  int((pops[0] != pops[1]).sum()))
+
+
 @pytest.mark.parametrize("q", [15, 19, 27])
 @pytest.mark.parametrize("cs", [0.0, 0.1])
 def test_fixed_point_path_runs_and_falls_back(q, cs):

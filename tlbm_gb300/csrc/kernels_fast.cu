@@ -49,6 +49,24 @@ __global__ void __launch_bounds__(128, 1) k_step_fast2(StepArgs a) {
   cell_step2<L, K, kClosure, kReg>(a, x, y0, y1 < a.pb.ny ? y1 : -1, z);
 }
 
+// 16-bit storage, cells in x pairs (step_fast.cuh: pair_step): thread (tx, ty) of a block of
+// (bx, by) takes cells 2 (bx * blockIdx.x + tx) and the next of row by * blockIdx.y + ty.  For
+// lattices with nx even and steps without time averaging.
+#ifndef TLBM_PAIRS_16
+#define TLBM_PAIRS_16 1
+#endif
+#ifndef TLBM_PAIR_MIN_BLOCKS
+#define TLBM_PAIR_MIN_BLOCKS 1
+#endif
+template <class L, int K, int kClosure>
+__global__ void __launch_bounds__(128, TLBM_PAIR_MIN_BLOCKS)
+    k_step_pair16(const __grid_constant__ PairArgs pa) {
+  const int x = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= pa.a.pb.nx || y >= pa.a.pb.ny) return;
+  pair_step<L, K, kClosure>(pa, x, y, blockIdx.z);
+}
+
 // FP64 storage with the fluid collision in exact fixed point (step_fast.cuh: cell_step_fx).  The
 // parameter is a __grid_constant__, so the out-of-line FP64 cold path takes it by reference
 // without a per-thread copy.  The kernel is bound by integer issue and dependent-latency stalls:
@@ -289,7 +307,25 @@ cudaError_t step_lk(const StepArgs& a, const Launch& l) {
   } else if ((K == kStoreBF16 || K == kStoreF16) && !a.pb.mcoll) {
     // 16-bit storage of f - w
     if constexpr (K == kStoreBF16 || K == kStoreF16) {
-      if (TLBM_TWO_CELLS_16) {
+      if (TLBM_PAIRS_16 && a.pb.nx % 2 == 0 && !a.time_avg) {
+        // a block row of bx pairs spans 2 bx cells: narrower blocks for narrow lattices
+        int bx = l.bx;
+        while (bx > 16 && 2 * bx > a.pb.nx) bx /= 2;
+        const int by = (l.bx * l.by) / bx;
+        const dim3 gp((a.pb.nx / 2 + bx - 1) / bx, (a.pb.ny + by - 1) / by, a.pb.nz),
+            bp(bx, by, 1);
+        PairArgs pa{};
+        pa.a = a;
+        const size_t words = static_cast<size_t>(a.pb.n) / 2;  // of one population plane
+        for (int i = 0; i < L::Q; ++i) {
+          pa.src[i] = static_cast<const uint32_t*>(a.src) + i * words;
+          pa.dst[i] = static_cast<uint32_t*>(a.dst) + i * words;
+        }
+        if (a.pb.cs > 0)
+          k_step_pair16<L, K, fast::kClosureSmag><<<gp, bp, 0, l.stream>>>(pa);
+        else
+          k_step_pair16<L, K, fast::kClosureNone><<<gp, bp, 0, l.stream>>>(pa);
+      } else if (TLBM_TWO_CELLS_16) {
         const dim3 g2(g.x, (a.pb.ny + 2 * l.by - 1) / (2 * l.by), g.z);
         if (a.pb.cs > 0)
           k_step_fast2<L, K, fast::kClosureSmag, false><<<g2, b, 0, l.stream>>>(a);

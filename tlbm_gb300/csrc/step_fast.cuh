@@ -332,4 +332,124 @@ __device__ __forceinline__ void cell_step2(const StepArgs& a, int x, int y0, int
   cell_compute<L, K, kClosure, kReg>(a, x, y1, c1, t1, r1);
 }
 
+// ------------------------------------------------------------ 16-bit storage, cells in x pairs
+// Cells (x, x + 1) of one row per thread, x even.  With nx even, each population of the pair
+// is one aligned 32-bit word of its plane (cell x in the low half), so the pair moves with one
+// load and one store per speed where two cells of their own take two of each, and one
+// instruction converts both cells' results.  A speed with e_x = 0 pulls the word of its source
+// row whole; e_x = +1 pulls cells (x - 1, x), the high half of the word before the pair's and
+// the low half of the pair's own; e_x = -1 pulls (x + 1, x + 2), the high half of the pair's
+// word and the low half of the one after.  The solid bounce-back swaps opposite shifts after
+// widening them to float, which both 16-bit formats hold exactly, so it stays a bit copy.
+template <int K>
+struct Pair16;
+
+template <>
+struct Pair16<kStoreBF16> {
+  static __device__ __forceinline__ float lo(uint32_t w) { return __uint_as_float(w << 16); }
+  static __device__ __forceinline__ float hi(uint32_t w) {
+    return __uint_as_float(w & 0xFFFF0000u);
+  }
+  // (a, b) rounded to nearest even, a in the low half
+  static __device__ __forceinline__ uint32_t pack(float a, float b) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&v);
+  }
+};
+
+template <>
+struct Pair16<kStoreF16> {
+  static __device__ __forceinline__ float lo(uint32_t w) {
+    return __half2float(__ushort_as_half(static_cast<unsigned short>(w & 0xFFFFu)));
+  }
+  static __device__ __forceinline__ float hi(uint32_t w) {
+    return __half2float(__ushort_as_half(static_cast<unsigned short>(w >> 16)));
+  }
+  static __device__ __forceinline__ uint32_t pack(float a, float b) {
+    const __half2 v = __floats2half2_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&v);
+  }
+};
+
+// a pair with a node that is neither fluid nor solid (inlet, outlet, moving wall): each cell
+// through the one-cell code, which loads its own values again
+template <class L, int K, int kClosure>
+__device__ __noinline__ void pair_cold(const StepArgs& a, int x, int y, int z) {
+  cell_step<L, K, kClosure, false, true, false>(a, x, y, z);
+  cell_step<L, K, kClosure, false, true, false>(a, x + 1, y, z);
+}
+
+// one cell's shifts d (f - w), fluid or solid, collided or bounced back in place
+template <class L, int kClosure>
+__device__ __forceinline__ void pair_cell(const DevProblem& pb, uint32_t t, float (&d)[L::Q]) {
+  if (t == kFluid) {
+    float rho, ux, uy, uz;
+    fast::fluid_collide_shifted<L, kClosure>(d, Par<float>::omega(pb), Par<float>::cs(pb),
+                                             Par<float>::nu(pb), relaxes(pb), rho, ux, uy, uz);
+  } else {
+    float s[L::Q];
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) s[i] = d[L::bb(i)];
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) d[i] = s[i];
+  }
+}
+
+// The pair step's parameters: the step's, and each population plane's first word in both
+// buffers, so that a word's address is one multiply-add of its index onto a parameter.
+struct PairArgs {
+  StepArgs a;
+  const uint32_t* src[27];
+  uint32_t* dst[27];
+};
+
+// The step of cells (x, x + 1) of row y, plane z, for launches without time averaging.
+template <class L, int K, int kClosure>
+__device__ __forceinline__ void pair_step(const PairArgs& pa, int x, int y, int z) {
+  using PK = Pair16<K>;
+  constexpr int Q = L::Q;
+  const StepArgs& a = pa.a;
+  const DevProblem& pb = a.pb;
+  const int nx = pb.nx;
+  // cell offsets of the source rows y - e_y and planes z - e_z (periodic)
+  const int y0 = y * nx, z0 = z * pb.nxy;
+  const int ym = (y == 0 ? pb.ny - 1 : y - 1) * nx, yp = (y == pb.ny - 1 ? 0 : y + 1) * nx;
+  const int zm = (z == 0 ? pb.nz - 1 : z - 1) * pb.nxy;
+  const int zp = (z == pb.nz - 1 ? 0 : z + 1) * pb.nxy;
+  const int xl = x == 0 ? nx - 2 : x - 2;  // the word before the pair's (e_x = +1)
+  const int xr = x + 2 == nx ? 0 : x + 2;  // the word after it (e_x = -1)
+  uint32_t w[Q];
+#pragma unroll
+  for (int i = 0; i < Q; ++i) {
+    const int ex = L::ex(i), ey = L::ey(i), ez = L::ez(i);
+    const int row = (ey > 0 ? ym : (ey < 0 ? yp : y0)) + (ez > 0 ? zm : (ez < 0 ? zp : z0));
+    const uint32_t* __restrict__ pl = pa.src[i];
+    const uint32_t mid = __ldg(pl + (static_cast<uint32_t>(row + x) >> 1));
+    if (ex == 0)
+      w[i] = mid;
+    else if (ex > 0)
+      w[i] = __byte_perm(__ldg(pl + (static_cast<uint32_t>(row + xl) >> 1)), mid, 0x5432);
+    else
+      w[i] = __byte_perm(mid, __ldg(pl + (static_cast<uint32_t>(row + xr) >> 1)), 0x5432);
+  }
+  const int c = x + y0 + z0;
+  const uint32_t tt = *reinterpret_cast<const uint16_t*>(pb.nd_type + c);
+  const uint32_t t0 = tt & 0xFFu, t1 = tt >> 8;
+  if (((t0 > kSolid) | (t1 > kSolid)) != 0) {
+    pair_cold<L, K, kClosure>(a, x, y, z);
+    return;
+  }
+  float d0[Q], d1[Q];
+#pragma unroll
+  for (int i = 0; i < Q; ++i) {
+    d0[i] = PK::lo(w[i]);
+    d1[i] = PK::hi(w[i]);
+  }
+  pair_cell<L, kClosure>(pb, t0, d0);
+  pair_cell<L, kClosure>(pb, t1, d1);
+  const uint32_t cw = static_cast<uint32_t>(c) >> 1;
+#pragma unroll
+  for (int i = 0; i < Q; ++i) pa.dst[i][cw] = PK::pack(d0[i], d1[i]);
+}
+
 }  // namespace tlbm
