@@ -113,9 +113,20 @@ void run(bool smag, int n, unsigned seed) {
       f[i] = static_cast<double>(feq * (1 + 2e-3L * U(rng)));
     }
     collide_exact<L>(f, smag, omega, cs, want);
+    // the same populations held as Q1.62 (exact: every value is above 2^-10)
+    fx::i64 F[Q];
+    for (int i = 0; i < Q; ++i) F[i] = fx::store_of_f64(f[i]);
+    fx::i64 rq, jq[3];
+    const bool ok_q = smag ? fx::fluid_collide<L, true>(F, k, rq, jq)
+                           : fx::fluid_collide<L, false>(F, k, rq, jq);
     const bool ok = smag ? smagorinsky<L>(f, k) : bgk<L>(f, k);
     CHECK(ok, "D3Q%d cell %d outside the fixed-point ranges", Q, c);
+    CHECK(ok_q == ok, "D3Q%d cell %d: the stored form's guards differ", Q, c);
     if (!ok) continue;
+    // the stored form keeps the collided Q1.62 values; their nearest doubles are the double
+    // form's results
+    for (int i = 0; i < Q; ++i)
+      CHECK(fx::f64_of_store(F[i]) == f[i], "D3Q%d cell %d speed %d: stored form", Q, c, i);
     for (int i = 0; i < Q; ++i) {
       const double e = ulps(f[i], want[i]);
       worst = e > worst ? e : worst;
@@ -151,6 +162,23 @@ void conversions(unsigned seed) {
   CHECK(fx::from_f64(0.0) == 0 && fx::from_f64(-0.0) == 0 && fx::from_f64(1e-300) == 0, "zero");
   CHECK(fx::from_f64(1.5) == (static_cast<fx::i64>(3) << 61), "1.5");
   CHECK(fx::from_f64(-1.0) == -(static_cast<fx::i64>(1) << 62), "-1");
+  // Q1.62 storage: exact above 2^-10 and back, nearest (ties to even) below, NaN marker
+  for (int t = 0; t < 1000000; ++t) {
+    const double d = std::ldexp(U(rng), -static_cast<int>(rng() % 40));
+    const fx::i64 v = fx::store_of_f64(d);
+    const LD err = std::fabs(std::ldexp(static_cast<LD>(v), -62) - static_cast<LD>(d));
+    CHECK(err <= 0x1p-63L, "store_of_f64(%.17g)", d);
+    if (err == 0x1p-63L) CHECK((v & 1) == 0, "store_of_f64 tie %.17g", d);
+    if (std::fabs(d) >= 0x1p-10) CHECK(fx::f64_of_store(v) == d, "storage round trip %.17g", d);
+    if (fails > 10) return;
+  }
+  CHECK(fx::store_of_f64(1.9999999999999998) == 0x7FFFFFFFFFFFFC00LL, "below 2");
+  CHECK(fx::store_of_f64(-1.9999999999999998) == -0x7FFFFFFFFFFFFC00LL, "above -2");
+  CHECK(fx::store_of_f64(2.0) == fx::kStoreNaN && fx::store_of_f64(-2.0) == fx::kStoreNaN &&
+            fx::store_of_f64(NAN) == fx::kStoreNaN && fx::store_of_f64(INFINITY) == fx::kStoreNaN,
+        "out of range -> NaN marker");
+  CHECK(std::isnan(fx::f64_of_store(fx::kStoreNaN)), "NaN marker reads as NaN");
+  CHECK(fx::f64_of_store(fx::store_of_f64(0.0)) == 0.0 && fx::store_of_f64(-0.0) == 0, "zero");
   // 1/(2 rho) to 2^-59 over the accepted density range
   for (int t = 0; t < 200000; ++t) {
     const fx::i64 rq = static_cast<fx::i64>(std::ldexp(1.25 + 0.75 * U(rng), 59));
@@ -193,6 +221,28 @@ void guards() {
   CHECK(bgk<L>(f, k), "f_0 = 0.9 accepted");
   for (int i = 0; i < Q; ++i) f[i] = static_cast<double>(L::wlit(i));
   CHECK(bgk<L>(f, k), "state at rest accepted");
+  // the stored form's population guards
+  fx::i64 F[Q], rq, jq[3];
+  auto rest = [&]() {
+    for (int i = 0; i < Q; ++i) F[i] = fx::store_of_f64(static_cast<double>(L::wlit(i)));
+  };
+  rest();
+  F[0] = 1LL << 62;  // f_0 = 1
+  CHECK(!(fx::fluid_collide<L, false>(F, k, rq, jq)) && F[0] == (1LL << 62), "stored f_0 < 1");
+  rest();
+  F[0] = -1;
+  CHECK(!(fx::fluid_collide<L, false>(F, k, rq, jq)), "stored f_0 >= 0");
+  rest();
+  F[1] = 1LL << 61;  // 1/2
+  CHECK(!(fx::fluid_collide<L, false>(F, k, rq, jq)), "stored |f_i| < 1/2");
+  rest();
+  F[2] = -(1LL << 61);
+  CHECK(!(fx::fluid_collide<L, false>(F, k, rq, jq)), "stored |f_i| < 1/2 (negative)");
+  rest();
+  F[Q - 1] = fx::kStoreNaN;
+  CHECK(!(fx::fluid_collide<L, false>(F, k, rq, jq)), "stored NaN marker");
+  rest();
+  CHECK((fx::fluid_collide<L, false>(F, k, rq, jq)), "stored state at rest accepted");
 }
 
 int main(int argc, char** argv) {

@@ -338,8 +338,14 @@ Status Engine::init(const int32_t* nd_type, const int32_t* parts, int size) {
     return Status::err(TLBM_ERR_INVALID_ARGUMENT, "mrt_ghost_rate must lie in (0, 2)");
   if (opt_.closure != TLBM_CLOSURE_PARAMS)
     return Status::err(TLBM_ERR_UNSUPPORTED, "closure option not available");
+  // FP64 in fast arithmetic: fluid nodes collide in exact fixed point (physics_fx.cuh), and the
+  // populations stay in its Q1.62 format between steps unless a moment-space collision runs
+  fx_ = store_ == kStoreF64 && !ref_arith_ && !opt_.f64_pipe &&
+        fx_collision_ok(prob_.omega, prob_.cs);
+  const bool mcoll = (opt_.rbgk && prob_.dynamics == 2) || (opt_.mrt && prob_.dynamics == 3);
+  if (fx_ && !mcoll && fx_storage_ok(prob_.omega, prob_.cs, prob_.rho_lbm)) store_ = kStoreFX;
   sb_ = store_bytes(store_);
-  ob_ = (store_ == kStoreF64) ? 8 : 4;
+  ob_ = (store_ == kStoreF64 || store_ == kStoreFX) ? 8 : 4;
 
   // node types: the reference's codes only (python/FluidChannel.py:1386-1397); checked and
   // narrowed to bytes in chunks on several host threads (33.5 M nodes take ~30 ms on one core)
@@ -491,12 +497,7 @@ Status Engine::init(const int32_t* nd_type, const int32_t* parts, int size) {
   }
   pb_.has_type5 = has_type5_ ? 1 : 0;
   fill_derived(pb_, q_, sb_);
-  // fluid collision in exact fixed point (physics_fx.cuh) for FP64 storage in fast arithmetic;
-  // its rate constants need 0 < omega < 2 (nu > 0)
-  pb_.fx = (store_ == kStoreF64 && !ref_arith_ && !opt_.f64_pipe && prob_.omega > 0.0 &&
-            prob_.omega < 2.0 && prob_.cs >= 0.0)
-               ? 1
-               : 0;
+  pb_.fx = fx_ ? 1 : 0;
   if (pb_.fx) fx::fill_consts(pb_.fxk, prob_.omega, prob_.cs, pb_.nu);
 
   const int nb = mass_blocks(pb_);

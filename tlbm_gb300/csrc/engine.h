@@ -95,6 +95,7 @@ class Engine {
   bool ref_arith_ = true;
   int sms_ = 0;  // multiprocessors of the device (set on first use)
   int store_ = kStoreF32;
+  bool fx_ = false;  // FP64 fluid nodes collided in fixed point
   int sb_ = 4;  // bytes per stored population
   int ob_ = 4;  // bytes per output value
   int64_t n_ = 0;

@@ -66,8 +66,16 @@ Status Ensemble::init(int n, const tlbm_problem* probs, const int32_t* const* nd
       return Status::err(TLBM_ERR_UNSUPPORTED, "ensembles take f64, f32, bf16 or f16 storage");
     default: return Status::err(TLBM_ERR_INVALID_ARGUMENT, "unknown precision option");
   }
+  // FP64 channels: populations held as Q1.62 when every channel's collision runs in fixed point
+  // with a density inside that format's range, as a single-lattice handle of each would
+  if (store_ == kStoreF64 && !opt_.f64_pipe) {
+    bool all = true;
+    for (int k = 0; k < n; ++k)
+      all &= fx_storage_ok(probs[k].omega, probs[k].cs, probs[k].rho_lbm);
+    if (all) store_ = kStoreFX;
+  }
   sb_ = store_bytes(store_);
-  ob_ = store_ == kStoreF64 ? 8 : 4;
+  ob_ = (store_ == kStoreF64 || store_ == kStoreFX) ? 8 : 4;
   prob_.assign(probs, probs + n);
   ch_.resize(n);
   size_t total = 0;
@@ -111,8 +119,8 @@ Status Ensemble::init(int n, const tlbm_problem* probs, const int32_t* const* nd
     pb.has_type5 = 0;
     fill_derived(pb, q, sb_);
     // FP64 channels collide fluid nodes in exact fixed point, as a single-lattice handle does
-    pb.fx = (store_ == kStoreF64 && !opt_.f64_pipe && p.omega > 0.0 && p.omega < 2.0 &&
-             p.cs >= 0.0)
+    pb.fx = ((store_ == kStoreF64 || store_ == kStoreFX) && !opt_.f64_pipe &&
+             fx_collision_ok(p.omega, p.cs))
                 ? 1
                 : 0;
     if (pb.fx) fx::fill_consts(pb.fxk, p.omega, p.cs, pb.nu);

@@ -16,8 +16,20 @@ enum StoreKind : int {
   kStoreBF16 = 2,
   kStoreF16 = 3,
   kStoreBF16M = 4,  // BF16 remainders after a per-cell moment shift (storage.cuh)
+  kStoreFX = 5,     // FP64 populations held as 64-bit fixed point, Q1.62 (storage.cuh)
 };
-inline int store_bytes(int k) { return k == kStoreF64 ? 8 : (k == kStoreF32 ? 4 : 2); }
+inline int store_bytes(int k) {
+  return (k == kStoreF64 || k == kStoreFX) ? 8 : (k == kStoreF32 ? 4 : 2);
+}
+// FP64 populations in fast arithmetic: the fluid collision runs in fixed point when its rate
+// constants exist (0 < omega < 2, cs >= 0); the populations are held as Q1.62 (kStoreFX) when,
+// in addition, the run's density keeps them well inside its range |f| < 2
+inline bool fx_collision_ok(double omega, double cs) {
+  return omega > 0.0 && omega < 2.0 && cs >= 0.0;
+}
+inline bool fx_storage_ok(double omega, double cs, double rho) {
+  return fx_collision_ok(omega, cs) && rho >= 0.5 && rho < 2.0;
+}
 // bytes of one population buffer: Q planes, then (moment-shifted kind) a float4 per cell
 inline size_t buffer_bytes(int k, int q, int64_t n) {
   const size_t planes = static_cast<size_t>(n) * q * store_bytes(k);

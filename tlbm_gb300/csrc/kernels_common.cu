@@ -41,6 +41,8 @@ __global__ void k_init_uniform(DevProblem pb, void* fv, double rho) {
       if constexpr (S::kShifted) {
         const C w = weight<L, float>(i);
         f[i * n + c] = S::save(w * static_cast<C>(rho), w);
+      } else if constexpr (K == kStoreFX) {
+        f[i * n + c] = S::save(weight<L, C>(i) * static_cast<C>(rho), C(0));
       } else if constexpr (!S::kMoment) {
         // w[spd]*rho in `real` (src/TLBM_Partition.cpp:462-463)
         f[i * n + c] = weight<L, C>(i) * static_cast<C>(rho);
@@ -160,6 +162,8 @@ __global__ void __launch_bounds__(kThreads) k_mass_partial(DevProblem pb, const 
         cell += static_cast<double>(moment::load<L>(f, moment::params(fv, L::Q, n), n, i, c));
       else if constexpr (S::kShifted)
         cell += static_cast<double>(weight<L, float>(i)) + static_cast<double>(f[i * n + c]);
+      else if constexpr (K == kStoreFX)
+        cell += S::load(f[i * n + c], 0.0);
       else
         cell += static_cast<double>(f[i * n + c]);
     }
@@ -191,6 +195,7 @@ cudaError_t by_q_store(int q, int store, A&&... a) {
   TLBM_CASE_K(19, kStoreBF16) TLBM_CASE_K(19, kStoreF16) TLBM_CASE_K(27, kStoreF64)
   TLBM_CASE_K(27, kStoreF32) TLBM_CASE_K(27, kStoreBF16) TLBM_CASE_K(27, kStoreF16)
   TLBM_CASE_K(15, kStoreBF16M) TLBM_CASE_K(19, kStoreBF16M) TLBM_CASE_K(27, kStoreBF16M)
+  TLBM_CASE_K(15, kStoreFX) TLBM_CASE_K(19, kStoreFX) TLBM_CASE_K(27, kStoreFX)
 #undef TLBM_CASE_K
   return cudaErrorInvalidValue;
 }

@@ -21,6 +21,7 @@ __device__ __forceinline__ int fast_div(int n, FastDiv d) {
 
 template <int K>
 __global__ void __launch_bounds__(256) k_ensemble_step(EnsembleArgs a) {
+  constexpr bool kFx = K == kStoreF64 || K == kStoreFX;  // fluid nodes in fixed point
   for (int t = blockIdx.x; t < a.n_tiles; t += gridDim.x) {
     const EnsembleTile tile = a.tiles[t];
     const EnsembleChannel& ch = a.channels[tile.channel];
@@ -33,14 +34,14 @@ __global__ void __launch_bounds__(256) k_ensemble_step(EnsembleArgs a) {
       const int x = r - y * s.pb.nx;
       if (ch.q == 19) {
         if (s.pb.cs > 0)
-          cell_step<Lattice<19>, K, fast::kClosureSmag, false, true, K == kStoreF64>(s, x, y, tile.z);
+          cell_step<Lattice<19>, K, fast::kClosureSmag, false, true, kFx>(s, x, y, tile.z);
         else
-          cell_step<Lattice<19>, K, fast::kClosureNone, false, true, K == kStoreF64>(s, x, y, tile.z);
+          cell_step<Lattice<19>, K, fast::kClosureNone, false, true, kFx>(s, x, y, tile.z);
       } else {
         if (s.pb.cs > 0)
-          cell_step<Lattice<15>, K, fast::kClosureSmag, false, true, K == kStoreF64>(s, x, y, tile.z);
+          cell_step<Lattice<15>, K, fast::kClosureSmag, false, true, kFx>(s, x, y, tile.z);
         else
-          cell_step<Lattice<15>, K, fast::kClosureNone, false, true, K == kStoreF64>(s, x, y, tile.z);
+          cell_step<Lattice<15>, K, fast::kClosureNone, false, true, kFx>(s, x, y, tile.z);
       }
     }
   }
@@ -60,6 +61,7 @@ int resident_blocks(int threads) {
 int ensemble_resident_blocks(int store, int threads) {
   switch (store) {
     case kStoreF64: return resident_blocks<kStoreF64>(threads);
+    case kStoreFX: return resident_blocks<kStoreFX>(threads);
     case kStoreF32: return resident_blocks<kStoreF32>(threads);
     case kStoreBF16: return resident_blocks<kStoreBF16>(threads);
     case kStoreF16: return resident_blocks<kStoreF16>(threads);
@@ -72,6 +74,7 @@ cudaError_t launch_ensemble_step(int store, const EnsembleArgs& a, int threads, 
   const dim3 block(threads, 1, 1);
   switch (store) {
     case kStoreF64: k_ensemble_step<kStoreF64><<<grid, block, 0, s>>>(a); break;
+    case kStoreFX: k_ensemble_step<kStoreFX><<<grid, block, 0, s>>>(a); break;
     case kStoreF32: k_ensemble_step<kStoreF32><<<grid, block, 0, s>>>(a); break;
     case kStoreBF16: k_ensemble_step<kStoreBF16><<<grid, block, 0, s>>>(a); break;
     case kStoreF16: k_ensemble_step<kStoreF16><<<grid, block, 0, s>>>(a); break;

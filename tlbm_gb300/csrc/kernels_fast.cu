@@ -78,14 +78,14 @@ __global__ void __launch_bounds__(128, TLBM_PAIR_MIN_BLOCKS)
 template <class L>
 constexpr int kFxMinBlocks = L::Q == 27 ? 4 : TLBM_FX_MIN_BLOCKS;
 
-template <class L, int kClosure>
+template <class L, int K, int kClosure>
 __global__ void __launch_bounds__(128, kFxMinBlocks<L>)
     k_step_fast_fx(const __grid_constant__ StepArgs a) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
   if (x >= a.pb.nx || y >= a.pb.ny) return;
-  cell_step_fx<L, kClosure>(a, x, y, z);
+  cell_step_fx<L, K, kClosure>(a, x, y, z);
 }
 
 // an opaque copy: the compiler cannot reuse values computed from v before this point
@@ -101,7 +101,7 @@ __device__ __forceinline__ void launder(double& v) { asm volatile("" : "+d"(v));
 #define TLBM_MLP_MIN_BLOCKS 8  // resident blocks per SM: 64 registers per thread
 #endif
 template <int K>
-constexpr int kMlpMinBlocks = K == kStoreF64 ? 4 : TLBM_MLP_MIN_BLOCKS;
+constexpr int kMlpMinBlocks = (K == kStoreF64 || K == kStoreFX) ? 4 : TLBM_MLP_MIN_BLOCKS;
 
 // One cell of the learned-closure step; all 32 lanes of the warp call it together (the network
 // is warp-collective), lanes outside the lattice included.  kReg: regularised (moment-space)
@@ -296,13 +296,13 @@ cudaError_t step_lk(const StepArgs& a, const Launch& l) {
       k_step_fast_mlp<L, K, true><<<g, b, 0, l.stream>>>(a, cl);
     else
       k_step_fast_mlp<L, K, false><<<g, b, 0, l.stream>>>(a, cl);
-  } else if (K == kStoreF64 && a.pb.fx && !a.pb.mcoll) {
-    // FP64 storage: fluid nodes in exact fixed point (physics_fx.cuh)
-    if constexpr (K == kStoreF64) {
+  } else if ((K == kStoreF64 || K == kStoreFX) && a.pb.fx && !a.pb.mcoll) {
+    // FP64 storage (double or Q1.62): fluid nodes in exact fixed point (physics_fx.cuh)
+    if constexpr (K == kStoreF64 || K == kStoreFX) {
       if (a.pb.cs > 0)
-        k_step_fast_fx<L, fast::kClosureSmag><<<g, b, 0, l.stream>>>(a);
+        k_step_fast_fx<L, K, fast::kClosureSmag><<<g, b, 0, l.stream>>>(a);
       else
-        k_step_fast_fx<L, fast::kClosureNone><<<g, b, 0, l.stream>>>(a);
+        k_step_fast_fx<L, K, fast::kClosureNone><<<g, b, 0, l.stream>>>(a);
     }
   } else if ((K == kStoreBF16 || K == kStoreF16) && !a.pb.mcoll) {
     // 16-bit storage of f - w
@@ -394,6 +394,9 @@ cudaError_t force_lk(const DevProblem& pb, const void* f, void* const out[3], co
       case 154: return FN<Lattice<15>, kStoreBF16M>(__VA_ARGS__);                   \
       case 194: return FN<Lattice<19>, kStoreBF16M>(__VA_ARGS__);                   \
       case 274: return FN<Lattice<27>, kStoreBF16M>(__VA_ARGS__);                   \
+      case 155: return FN<Lattice<15>, kStoreFX>(__VA_ARGS__);                      \
+      case 195: return FN<Lattice<19>, kStoreFX>(__VA_ARGS__);                      \
+      case 275: return FN<Lattice<27>, kStoreFX>(__VA_ARGS__);                      \
       default: return cudaErrorInvalidValue;                                        \
     }                                                                               \
   } while (0)

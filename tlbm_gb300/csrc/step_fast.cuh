@@ -225,26 +225,29 @@ template <class L, int K, int kClosure, bool kReg = false, bool kWrapFree = true
           bool kFx = false>
 __device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z);
 
-// FP64 storage, the FP64 code for one cell, out of line: the fixed-point kernel sends here the
-// nodes its hot path does not take (boundary nodes, fluid nodes outside the fixed-point ranges,
-// runs that accumulate time averages), which reload their populations.
-template <class L, int kClosure>
+// FP64 storage (double or Q1.62), the FP64 code for one cell, out of line: the fixed-point
+// kernel sends here the nodes its hot path does not take (boundary nodes, fluid nodes outside
+// the fixed-point ranges, runs that accumulate time averages), which reload their populations.
+template <class L, int K, int kClosure>
 __device__ __noinline__ void cell_step_f64_cold(const StepArgs& a, int x, int y, int z) {
-  cell_step<L, kStoreF64, kClosure, false, true, false>(a, x, y, z);
+  cell_step<L, K, kClosure, false, true, false>(a, x, y, z);
 }
 
 // FP64 storage with the fluid collision in exact fixed point (physics_fx.cuh): solid nodes swap
-// and fluid nodes collide here; everything else goes to cell_step_f64_cold.  The hot path holds
-// no FP64 arithmetic, so it stays small for the instruction cache.
-template <class L, int kClosure>
+// and fluid nodes collide here; everything else goes to cell_step_f64_cold.  With Q1.62 storage
+// (kStoreFX) the populations move between HBM and the collision as they are; with double
+// storage each converts exactly in and to the nearest double out.  The hot path holds no FP64
+// arithmetic, so it stays small for the instruction cache.
+template <class L, int K, int kClosure>
 __device__ __forceinline__ void cell_step_fx(const StepArgs& a, int x, int y, int z) {
+  using T = typename Store<K>::T;
   const DevProblem& pb = a.pb;
   const int c = x + y * pb.nx + z * pb.nxy;
-  double f[L::Q];
-  load_raw<L, kStoreF64, true>(a, x, y, z, c, f);
+  T f[L::Q];
+  load_raw<L, K, true>(a, x, y, z, c, f);
   const uint8_t t = pb.nd_type[c];
   if (!a.time_avg && pb.fx) {
-    double* __restrict__ dst = static_cast<double*>(a.dst);
+    T* __restrict__ dst = static_cast<T*>(a.dst);
     const size_t n = static_cast<size_t>(pb.n);
     if (t == kSolid) {
 #pragma unroll
@@ -259,7 +262,7 @@ __device__ __forceinline__ void cell_step_fx(const StepArgs& a, int x, int y, in
       return;
     }
   }
-  cell_step_f64_cold<L, kClosure>(a, x, y, z);
+  cell_step_f64_cold<L, K, kClosure>(a, x, y, z);
 }
 
 // the part of cell_step after the loads: node-type branch, collision, store
@@ -299,8 +302,8 @@ __device__ __forceinline__ void cell_compute(const StepArgs& a, int x, int y, in
 
 template <class L, int K, int kClosure, bool kReg, bool kWrapFree, bool kFx>
 __device__ __forceinline__ void cell_step(const StepArgs& a, int x, int y, int z) {
-  if constexpr (kFx && K == kStoreF64 && !kReg) {
-    cell_step_fx<L, kClosure>(a, x, y, z);
+  if constexpr (kFx && (K == kStoreF64 || K == kStoreFX) && !kReg) {
+    cell_step_fx<L, K, kClosure>(a, x, y, z);
   } else {
     const DevProblem& pb = a.pb;
     const int c = x + y * pb.nx + z * pb.nxy;

@@ -8,6 +8,9 @@
 //                are the density and momentum of the populations the cell s that stored them
 //                held after its collision; (rho_s, 3 j_s) follow the Q planes as one float4 per
 //                cell.
+//   kStoreFX   : FP64 populations as 64-bit fixed point Q1.62 (physics_fx.cuh), fluid nodes
+//                collided in fixed point as stored, everything else computed in double after
+//                a conversion to the nearest double (and back to the nearest Q1.62).
 // Storing f_i - w_i keeps the 16-bit mantissa on the part that varies: at rest f_i == w_i and
 // the stored value is 0, so the round-off scales with the deviation, not with w_i.  The
 // moment shift also removes the first-order part w_i 3 e_i.j: the remainder is the second-order
@@ -77,6 +80,17 @@ struct Store<kStoreF16> {
   static __device__ __forceinline__ T save(C f, C w) { return __float2half_rn(f - w); }
   static __device__ __forceinline__ C shift_of(T v) { return __half2float(v); }
   static __device__ __forceinline__ T of_shift(C d) { return __float2half_rn(d); }
+};
+
+template <>
+struct Store<kStoreFX> {
+  using T = fx::i64;
+  using P = T;
+  static constexpr bool kMoment = false;
+  using C = double;
+  static constexpr bool kShifted = false;
+  static __device__ __forceinline__ C load(T v, C) { return fx::f64_of_store(v); }
+  static __device__ __forceinline__ T save(C f, C) { return fx::store_of_f64(f); }
 };
 
 template <>
