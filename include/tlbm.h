@@ -84,10 +84,13 @@ typedef struct tlbm_options {
   float mrt_ghost_rate; /* ghost-moment rate in (0, 2), a float; <= 0 selects 1.2.  The rate
                            omega gives BGK, 1 the regularised collision. */
   int f64_pipe;    /* TLBM_PREC_F64 with TLBM_ARITH_FAST: 0 (default) collides fluid nodes in
-                      exact 64-bit fixed point (double-float for the Smagorinsky rate) and rounds
-                      each result once to double, so no FP64 instruction runs on the fluid path;
-                      1 collides them in FP64 arithmetic on the FP64 pipe, as boundary nodes
-                      always are.  Both meet the same bar against the reference arithmetic. */
+                      exact 64-bit fixed point (double-float for the Smagorinsky rate), so no
+                      FP64 instruction runs on the fluid path, and for rho_lbm in [1/2, 2) holds
+                      the populations on the device as that fixed point (Q1.62; exports give
+                      the nearest double, and a population of magnitude 2 or more reads back as
+                      NaN); 1 collides them in FP64 arithmetic on the FP64 pipe, as boundary
+                      nodes always are, with IEEE double storage.  Both meet the same bar
+                      against the reference arithmetic. */
   int reserved[5];
 } tlbm_options;
 
