@@ -406,13 +406,12 @@ struct PairArgs {
   uint32_t* dst[27];
 };
 
-// The step of cells (x, x + 1) of row y, plane z, for launches without time averaging.
-template <class L, int K, int kClosure>
-__device__ __forceinline__ void pair_step(const PairArgs& pa, int x, int y, int z) {
-  using PK = Pair16<K>;
-  constexpr int Q = L::Q;
-  const StepArgs& a = pa.a;
-  const DevProblem& pb = a.pb;
+// The populations (one word per speed) and the two node types of cells (x, x + 1), row y,
+// plane z.
+template <class L>
+__device__ __forceinline__ void pair_load(const PairArgs& pa, int x, int y, int z,
+                                          uint32_t (&w)[L::Q], uint32_t& tt) {
+  const DevProblem& pb = pa.a.pb;
   const int nx = pb.nx;
   // cell offsets of the source rows y - e_y and planes z - e_z (periodic)
   const int y0 = y * nx, z0 = z * pb.nxy;
@@ -421,9 +420,8 @@ __device__ __forceinline__ void pair_step(const PairArgs& pa, int x, int y, int 
   const int zp = (z == pb.nz - 1 ? 0 : z + 1) * pb.nxy;
   const int xl = x == 0 ? nx - 2 : x - 2;  // the word before the pair's (e_x = +1)
   const int xr = x + 2 == nx ? 0 : x + 2;  // the word after it (e_x = -1)
-  uint32_t w[Q];
 #pragma unroll
-  for (int i = 0; i < Q; ++i) {
+  for (int i = 0; i < L::Q; ++i) {
     const int ex = L::ex(i), ey = L::ey(i), ez = L::ez(i);
     const int row = (ey > 0 ? ym : (ey < 0 ? yp : y0)) + (ez > 0 ? zm : (ez < 0 ? zp : z0));
     const uint32_t* __restrict__ pl = pa.src[i];
@@ -435,11 +433,19 @@ __device__ __forceinline__ void pair_step(const PairArgs& pa, int x, int y, int 
     else
       w[i] = __byte_perm(mid, __ldg(pl + (static_cast<uint32_t>(row + xr) >> 1)), 0x5432);
   }
-  const int c = x + y0 + z0;
-  const uint32_t tt = *reinterpret_cast<const uint16_t*>(pb.nd_type + c);
+  tt = *reinterpret_cast<const uint16_t*>(pb.nd_type + x + y0 + z0);
+}
+
+// The rest of the step of cells (x, x + 1) from their loaded words and types.
+template <class L, int K, int kClosure>
+__device__ __forceinline__ void pair_finish(const PairArgs& pa, int x, int y, int z,
+                                            const uint32_t (&w)[L::Q], uint32_t tt) {
+  using PK = Pair16<K>;
+  constexpr int Q = L::Q;
+  const DevProblem& pb = pa.a.pb;
   const uint32_t t0 = tt & 0xFFu, t1 = tt >> 8;
   if (((t0 > kSolid) | (t1 > kSolid)) != 0) {
-    pair_cold<L, K, kClosure>(a, x, y, z);
+    pair_cold<L, K, kClosure>(pa.a, x, y, z);
     return;
   }
   float d0[Q], d1[Q];
@@ -450,9 +456,17 @@ __device__ __forceinline__ void pair_step(const PairArgs& pa, int x, int y, int 
   }
   pair_cell<L, kClosure>(pb, t0, d0);
   pair_cell<L, kClosure>(pb, t1, d1);
-  const uint32_t cw = static_cast<uint32_t>(c) >> 1;
+  const uint32_t cw = static_cast<uint32_t>(x + y * pb.nx + z * pb.nxy) >> 1;
 #pragma unroll
   for (int i = 0; i < Q; ++i) pa.dst[i][cw] = PK::pack(d0[i], d1[i]);
+}
+
+// The step of cells (x, x + 1) of row y, plane z, for launches without time averaging.
+template <class L, int K, int kClosure>
+__device__ __forceinline__ void pair_step(const PairArgs& pa, int x, int y, int z) {
+  uint32_t w[L::Q], tt;
+  pair_load<L>(pa, x, y, z, w, tt);
+  pair_finish<L, K, kClosure>(pa, x, y, z, w, tt);
 }
 
 }  // namespace tlbm
