@@ -116,10 +116,10 @@ def workload(args):
     return g, p
 
 
-def cpu_sample(g, p):
-    """A z-slab of the workload for the CPU baseline: first CPU_SAMPLE_NZ planes of the pack,
-    inlet plane kept, last plane turned into the outlet."""
-    nz = min(CPU_SAMPLE_NZ, g.nz)
+def cpu_sample(g, p, planes=CPU_SAMPLE_NZ):
+    """A z-slab of the workload for the CPU baseline: its first `planes` planes, inlet plane
+    kept, last plane turned into the outlet."""
+    nz = min(planes, g.nz)
     nd = g.nd_type.reshape(g.nz, g.ny, g.nx)[:nz].copy()
     nd[-1][nd[-1] != 1] = 3
     return nd.reshape(-1), nz
@@ -252,15 +252,14 @@ def traffic_per_cell(lattice, precision, arithmetic):
 # ----------------------------------------------------------------------------- arms
 
 
-def cpu_baseline(g, p, seconds=10.0, chunk=10, warmup=2):
-    """The CPU restatement of the reference timestep on all host cores, on a z-slab of the
-    workload, timed over whole chunks of steps until `seconds` of work have passed."""
+def _time_port(g, p, nz, threads, seconds, chunk, warmup):
+    """MLUPS of the C restatement of the reference timestep on the first nz planes of the
+    workload (cpu_sample), `threads` OpenMP threads, whole chunks of steps until `seconds`."""
     sys.path.insert(0, os.path.join(HERE, "tests"))
     import oracle_lib
 
-    nd, nz = cpu_sample(g, p)
+    nd, nz = cpu_sample(g, p, nz)
     q = int(p.lattice[3:])
-    threads = os.cpu_count() or 1
     o = oracle_lib.Oracle(q, 1, p.cs, p.rho_lbm, p.u_lbm, p.omega, g.nx, g.ny, nz, nd,
                           prec="f64", threads=threads)
     o.run(warmup)
@@ -273,9 +272,18 @@ def cpu_baseline(g, p, seconds=10.0, chunk=10, warmup=2):
         if dt >= seconds:
             break
     o.close()
-    cells = g.nx * g.ny * nz
+    return g.nx * g.ny * nz * steps / dt / 1e6, nz, steps, dt
+
+
+def cpu_baseline(g, p, seconds=10.0, chunk=10, warmup=2):
+    """The CPU restatement of the reference timestep on all host cores, on a z-slab of the
+    workload, timed over whole chunks of steps until `seconds` of work have passed; and the same
+    on one core (one MPI rank of the reference), on a thinner slab."""
+    threads = os.cpu_count() or 1
+    value, nz, steps, dt = _time_port(g, p, CPU_SAMPLE_NZ, threads, seconds, chunk, warmup)
+    v1, nz1, steps1, dt1 = _time_port(g, p, 4, 1, seconds / 2, 2, 1)
     return {
-        "value": round(cells * steps / dt / 1e6, 3),
+        "value": round(value, 3),
         "unit": "MLUPS",
         "cores": threads,
         "kind": "port",
@@ -283,6 +291,9 @@ def cpu_baseline(g, p, seconds=10.0, chunk=10, warmup=2):
                   "%d timed steps (%.1f s) of the C restatement of the reference timestep "
                   "(AoS push, int32 neighbour table), OpenMP over nodes"
                   % (g.nx, g.ny, nz, p.lattice, warmup, steps, dt),
+        "single_core": {"value": round(v1, 3), "unit": "MLUPS", "cores": 1,
+                        "sample": "%dx%dx%d slab, 1 warm-up + %d timed steps (%.1f s), one thread"
+                                  % (g.nx, g.ny, nz1, steps1, dt1)},
     }
 
 
