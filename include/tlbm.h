@@ -239,19 +239,19 @@ tlbm_status tlbm_load_restart(tlbm_handle* h, const float* ux, const float* uy, 
  * float32 inputs): u / (t_conv/l_conv), rho * p_conv - pRef, |u|, F * l_conv/u_conv^2; time
  * averages are first divided by Num_ts.  Output planes, n = nx*ny*nz floats each, in the order
  * of the datasets of hdf5Helper.writeH5 (python/hdf5Helper.py:4-31): ux, uy, uz, |u|, Fx, Fy,
- * Fz, pressure (8 planes); time averages: ux, uy, uz, |u|, pressure (5 planes).  The files
- * replace out{n}.h5 / timeAvg.h5 (HDF5 is not available here) by raw little-endian float32
- * out{n}.bin / timeAvg.bin in that plane order, and data{n}.xmf / timeAvg.xmf are the XDMF of
- * writeXdmf (hdf5Helper.py:58-202) with Format="Binary" items at byte offsets. */
+ * Fz, pressure (8 planes); time averages: ux, uy, uz, |u|, pressure (5 planes).  The files are
+ * the script's: out{n}.h5 / timeAvg.h5 with its groups and float32 datasets (velo_group,
+ * force_group, pres_group; pressure and |u| shaped nz x ny x nx), written without an HDF5
+ * library, and data{n}.xmf / timeAvg.xmf, the XDMF of writeXdmf (hdf5Helper.py:58-202). */
 
 /* The processed planes of the last step (time_avg = 0) or of the time-average sums
  * (time_avg = 1, needs params.lbm line 15 = 1) into host memory `out`.  FP64 runs round their
  * values to float32 first. */
 tlbm_status tlbm_processed_fields(tlbm_handle* h, int time_avg, float* out);
 
-/* The same, written in the handle's directory: out{k}.bin + data{k}.xmf for k = 0, 1, ... (one
+/* The same, written in the handle's directory: out{k}.h5 + data{k}.xmf for k = 0, 1, ... (one
  * per call, matching the dump numbers when called once per tlbm_write_data), or
- * timeAvg.bin + timeAvg.xmf.  In-situ: the raw dump files are not needed. */
+ * timeAvg.h5 + timeAvg.xmf.  In-situ: the raw dump files are not needed. */
 tlbm_status tlbm_write_processed_data(tlbm_handle* h, int time_avg);
 
 /* Replaces running processTLBM.py in a finished run's directory: reads params.lbm,

@@ -410,7 +410,7 @@ class TLBMPartition:
         return {k: out[i * n:(i + 1) * n].reshape(nz, ny, nx) for i, k in enumerate(names)}
 
     def write_processed_data(self, time_avg: bool = False) -> None:
-        """out{k}.bin + data{k}.xmf (or timeAvg.bin/.xmf) in the run directory."""
+        """out{k}.h5 + data{k}.xmf (or timeAvg.h5/.xmf) in the run directory."""
         _check(self._L.tlbm_write_processed_data(self._h, int(bool(time_avg))), self._h)
 
     def _shape(self):

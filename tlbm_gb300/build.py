@@ -43,6 +43,7 @@ UNITS = [
     ("kernels_mlp.cu", []),
     ("kernels_post.cu", ["-fmad=false"]),
     ("post.cpp", ["-x", "cu"]),
+    ("h5lite.cpp", ["-x", "cu"]),
     ("mlp_trainer.cpp", ["-x", "cu"]),
     ("capi_mlp.cpp", ["-x", "cu"]),
     ("engine.cpp", ["-x", "cu"]),

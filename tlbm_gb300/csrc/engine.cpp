@@ -23,6 +23,7 @@
 #include <sstream>
 #include <thread>
 
+#include "h5lite.h"
 #include "mlp.cuh"
 #include "mlp_kernels.h"
 #include "post.h"
@@ -511,25 +512,39 @@ Status Engine::init(const int32_t* nd_type, const int32_t* parts, int size) {
   }
   TLBM_CUDA(cudaStreamSynchronize(stream_));
   if (prob_.restart_flag) {
-    // load_restart_data (src/TLBM_Partition.cpp:481-540) reads restart.h5; the same four
-    // datasets are read here as raw float32 files in global node order
+    // load_restart_data (src/TLBM_Partition.cpp:481-540): the datasets velocity/{x,y,z} and
+    // density/rho of restart.h5, read as NATIVE_FLOAT in global node order; without
+    // restart.h5, the same four fields as raw float32 files restart_{ux,uy,uz,rho}.b_dat
     if (workdir_.empty())
       return Status::err(TLBM_ERR_INVALID_ARGUMENT,
                          "restart flag set without a directory: use tlbm_load_restart");
-    const char* names[4] = {"restart_ux.b_dat", "restart_uy.b_dat", "restart_uz.b_dat",
-                            "restart_rho.b_dat"};
     std::vector<std::vector<float>> r(4);
-    for (int k = 0; k < 4; ++k) {
-      std::string bytes;
-      Status s = read_text(workdir_ + "/" + names[k], &bytes);
-      if (!s.good())
-        return Status::err(TLBM_ERR_IO, std::string("restart data: ") + s.msg +
-                                            " (restart.h5 is HDF5, not read here; write the four "
-                                            "datasets as restart_{ux,uy,uz,rho}.b_dat)");
-      if (bytes.size() != n * sizeof(float))
-        return Status::err(TLBM_ERR_FORMAT, std::string(names[k]) + " must hold nx*ny*nz floats");
-      r[k].resize(n);
-      std::memcpy(r[k].data(), bytes.data(), bytes.size());
+    const std::string h5file = workdir_ + "/restart.h5";
+    if (std::ifstream(h5file).good()) {
+      const char* sets[4] = {"velocity/x", "velocity/y", "velocity/z", "density/rho"};
+      for (int k = 0; k < 4; ++k) {
+        std::vector<uint64_t> dims;
+        const std::string e = h5::read_f32(h5file, sets[k], &r[k], &dims);
+        if (!e.empty()) return Status::err(TLBM_ERR_FORMAT, "restart data: " + e);
+        if (r[k].size() != n)
+          return Status::err(TLBM_ERR_FORMAT, "restart.h5: " + std::string(sets[k]) +
+                                                  " must hold nx*ny*nz values");
+      }
+    } else {
+      const char* names[4] = {"restart_ux.b_dat", "restart_uy.b_dat", "restart_uz.b_dat",
+                              "restart_rho.b_dat"};
+      for (int k = 0; k < 4; ++k) {
+        std::string bytes;
+        Status s = read_text(workdir_ + "/" + names[k], &bytes);
+        if (!s.good())
+          return Status::err(TLBM_ERR_IO, std::string("restart data: ") + s.msg +
+                                              " (and no restart.h5)");
+        if (bytes.size() != n * sizeof(float))
+          return Status::err(TLBM_ERR_FORMAT,
+                             std::string(names[k]) + " must hold nx*ny*nz floats");
+        r[k].resize(n);
+        std::memcpy(r[k].data(), bytes.data(), bytes.size());
+      }
     }
     TLBM_TRY(load_restart(r[0].data(), r[1].data(), r[2].data(), r[3].data()));
   }
@@ -811,9 +826,9 @@ Status Engine::write_processed(bool time_avg) {
   TLBM_TRY(processed(time_avg, host.data()));
   const std::string d = std::to_string(proc_num_);
   std::string err;
-  const bool ok = time_avg ? post_write(workdir_, "timeAvg.bin", "timeAvg.xmf", prob_,
+  const bool ok = time_avg ? post_write(workdir_, "timeAvg.h5", "timeAvg.xmf", prob_,
                                         host.data(), true, &err)
-                           : post_write(workdir_, "out" + d + ".bin", "data" + d + ".xmf", prob_,
+                           : post_write(workdir_, "out" + d + ".h5", "data" + d + ".xmf", prob_,
                                         host.data(), false, &err);
   if (!ok) return Status::err(TLBM_ERR_IO, err);
   if (!time_avg) ++proc_num_;

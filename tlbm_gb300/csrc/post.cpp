@@ -1,11 +1,10 @@
 // post.cpp -- processTLBM.py (python/processTLBM.py) over the dump files, with the unit
 // conversion on the GPU (kernels_post.cu), and the XDMF descriptions of its output.
 //
-// processTLBM stores its datasets in out{n}.h5 / timeAvg.h5 (python/hdf5Helper.py:4-56).  HDF5
-// is not available to this library, so the same datasets are stored as raw little-endian
-// float32 planes in out{n}.bin / timeAvg.bin and the XDMF files address them with
-// Format="Binary" and a byte offset instead of an HDF path; the grid, attribute names and
-// dimensions are those of writeXdmf / writeXdmf_time_avg (python/hdf5Helper.py:58-202).
+// processTLBM stores its datasets in out{n}.h5 / timeAvg.h5 (python/hdf5Helper.py:4-56): the
+// same groups and datasets are written here by h5lite.cpp (no HDF5 library), pressure and
+// |u| shaped (Nz, Ny, Nx) as processTLBM.py:118-120 reshapes them, the others flat; the XDMF
+// files are writeXdmf / writeXdmf_time_avg's (python/hdf5Helper.py:58-202) text.
 #include "post.h"
 
 #include <cmath>
@@ -17,6 +16,7 @@
 #include <vector>
 
 #include "engine.h"
+#include "h5lite.h"
 
 namespace tlbm {
 
@@ -51,28 +51,30 @@ std::string fmt(const char* f, ...) {
 
 }  // namespace
 
-std::string post_xdmf(const tlbm_problem& p, const std::string& bin_name, bool time_avg) {
+std::string post_xdmf(const tlbm_problem& p, const std::string& h5_name, bool time_avg) {
   const int nx = p.nx, ny = p.ny, nz = p.nz;
   // x = linspace(0, Lx_p, Nx); dx = x[1] - x[0] = Lx_p / (Nx - 1) (processTLBM.py:54, :62)
   const double dx = nx > 1 ? p.lx_p / (nx - 1) : 0.0;
-  const long long plane = static_cast<long long>(nx) * ny * nz * 4;
-  auto item = [&](int k) {
-    return fmt("<DataItem Dimensions=\"%d %d %d\" NumberType=\"Float\" Precision=\"4\" "
-               "Format=\"Binary\" Endian=\"Little\" Seek=\"%lld\">\n",
-               nz, ny, nx, plane * k) +
-           bin_name + "\n</DataItem>\n";
+  auto item = [&](const char* ds) {
+    return fmt("<DataItem Dimensions=\"%d %d %d\" NumberType=\"Float\" Format=\"HDF\">\n", nz,
+               ny, nx) +
+           h5_name + ":/" + ds + "\n</DataItem>\n";
   };
-  auto vector = [&](const char* name, int k0) {
+  auto vector = [&](const char* name, const char* const (&ds)[3]) {
     std::string s = fmt("<Attribute Name=\"%s\" AttributeType=\"Vector\" Center=\"Node\">\n", name);
     s += fmt("<DataItem ItemType=\"Function\" Function=\"JOIN($0, $1, $2)\" "
              "Dimensions=\"%d %d %d 3\">\n", nz, ny, nx);
-    for (int k = k0; k < k0 + 3; ++k) s += item(k);
+    for (const char* d : ds) s += item(d);
     return s + "</DataItem>\n</Attribute>\n";
   };
-  auto scalar = [&](const char* name, int k) {
+  auto scalar = [&](const char* name, const char* ds) {
     return fmt("<Attribute Name=\"%s\" AttributeType=\"Scalar\" Center=\"Node\">\n", name) +
-           item(k) + "</Attribute>\n";
+           item(ds) + "</Attribute>\n";
   };
+  static const char* const kVelo[3] = {"velo_group/x_velo", "velo_group/y_velo",
+                                       "velo_group/z_velo"};
+  static const char* const kForce[3] = {"force_group/x_force", "force_group/y_force",
+                                        "force_group/z_force"};
   std::string s = "<?xml version=\"1.0\" ?>\n<!DOCTYPE Xdmf SYSTEM \"Xdmf.dtd\" []>\n";
   s += "<Xdmf xmlns:xi=\"http://www.w3.org/2003/XInclude\" Version=\"2.1\">\n<Domain>\n";
   s += "<Grid Name=\"my_Grid\" GridType=\"Uniform\">\n";
@@ -82,33 +84,35 @@ std::string post_xdmf(const tlbm_problem& p, const std::string& bin_name, bool t
   s += "<DataItem Dimensions=\"3\" NumberType=\"Integer\" Format=\"XML\">\n0 0 0\n</DataItem>\n";
   s += "<DataItem Dimensions=\"3\" NumberType=\"Integer\" Format=\"XML\">\n";
   s += fmt("%g %g %g\n", dx, dx, dx) + "</DataItem>\n</Geometry>\n";
-  s += vector("velocity", kPostUx);
-  if (!time_avg) s += vector("force", kPostFx);
-  s += scalar("pressure", time_avg ? kPostAvgFields - 1 : kPostPressure);
-  s += scalar("velocityMagnitude", kPostVelmag);
+  s += vector("velocity", kVelo);
+  if (!time_avg) s += vector("force", kForce);
+  s += scalar("pressure", "pres_group/presmag");
+  s += scalar("velocityMagnitude", "velo_group/velmag");
   s += "</Grid>\n</Domain>\n</Xdmf>\n";
   return s;
 }
 
-bool post_write(const std::string& dir, const std::string& bin_name, const std::string& xmf_name,
+bool post_write(const std::string& dir, const std::string& h5_name, const std::string& xmf_name,
                 const tlbm_problem& p, const float* planes, bool time_avg, std::string* err) {
-  const size_t n = static_cast<size_t>(p.nx) * p.ny * p.nz;
-  const size_t count = n * (time_avg ? kPostAvgFields : kPostFields);
-  {
-    std::ofstream out(dir + "/" + bin_name, std::ios::binary | std::ios::trunc);
-    if (!out.is_open()) {
-      *err = "cannot open " + dir + "/" + bin_name + " for writing";
-      return false;
-    }
-    out.write(reinterpret_cast<const char*>(planes), static_cast<std::streamsize>(count * 4));
-    if (!out.good()) {
-      *err = "write failed: " + dir + "/" + bin_name;
-      return false;
-    }
+  const uint64_t n = static_cast<uint64_t>(p.nx) * p.ny * p.nz;
+  const std::vector<uint64_t> flat = {n};
+  const std::vector<uint64_t> grid = {static_cast<uint64_t>(p.nz), static_cast<uint64_t>(p.ny),
+                                      static_cast<uint64_t>(p.nx)};
+  auto plane = [&](int k) { return planes + static_cast<size_t>(k) * n; };
+  std::vector<h5::Dataset> sets = {{"velo_group/x_velo", flat, plane(kPostUx)},
+                                   {"velo_group/y_velo", flat, plane(kPostUy)},
+                                   {"velo_group/z_velo", flat, plane(kPostUz)},
+                                   {"velo_group/velmag", grid, plane(kPostVelmag)}};
+  if (!time_avg) {
+    sets.push_back({"force_group/x_force", flat, plane(kPostFx)});
+    sets.push_back({"force_group/y_force", flat, plane(kPostFy)});
+    sets.push_back({"force_group/z_force", flat, plane(kPostFz)});
   }
+  sets.push_back({"pres_group/presmag", grid,
+                  plane(time_avg ? kPostAvgFields - 1 : kPostPressure)});
+  if (!h5::write_f32(dir + "/" + h5_name, sets, err)) return false;
   std::ofstream x(dir + "/" + xmf_name, std::ios::trunc);
-  const std::string text = post_xdmf(p, bin_name, time_avg);
-  x << text;
+  x << post_xdmf(p, h5_name, time_avg);
   if (!x.good()) {
     *err = "write failed: " + dir + "/" + xmf_name;
     return false;
@@ -244,12 +248,12 @@ Status post_process_dir(const std::string& dir, int device, int* dumps_done) {
     s = run({"ux" + d + ".b_dat", "uy" + d + ".b_dat", "uz" + d + ".b_dat",
              "density" + d + ".b_dat", "Fx" + d + ".b_dat", "Fy" + d + ".b_dat",
              "Fz" + d + ".b_dat"},
-            false, "out" + d + ".bin", "data" + d + ".xmf");
+            false, "out" + d + ".h5", "data" + d + ".xmf");
     if (!s.good()) return s;
     ++*dumps_done;
   }
   if (p.time_avg_flag == 1) {
-    s = run({"uAvg.b_dat", "vAvg.b_dat", "wAvg.b_dat", "rhoAvg.b_dat"}, true, "timeAvg.bin",
+    s = run({"uAvg.b_dat", "vAvg.b_dat", "wAvg.b_dat", "rhoAvg.b_dat"}, true, "timeAvg.h5",
             "timeAvg.xmf");
     if (!s.good()) return s;
   }

@@ -10,8 +10,8 @@
 
 namespace tlbm {
 
-// planes of the processed output, in the order they are stored in out{n}.bin (the datasets of
-// writeH5, python/hdf5Helper.py:4-31); the time-average file holds planes 0-3 then pressure
+// planes of the processed output (the datasets of writeH5, python/hdf5Helper.py:4-31); the
+// time-average output holds planes 0-3 then pressure
 enum : int {
   kPostUx = 0,
   kPostUy = 1,
@@ -58,12 +58,14 @@ PostFactors post_factors(const tlbm_problem& p, bool time_avg);
 // processTLBM.py's number of dumps: int((Num_ts - Warmup_ts) / plot_freq) (:65, :70)
 int post_num_dumps(const tlbm_problem& p);
 
-// writeXdmf / writeXdmf_time_avg (python/hdf5Helper.py:58-202) for data in a raw little-endian
-// float32 file `bin_name` laid out as the planes above
-std::string post_xdmf(const tlbm_problem& p, const std::string& bin_name, bool time_avg);
+// writeXdmf / writeXdmf_time_avg (python/hdf5Helper.py:58-202): the XDMF text that describes
+// the datasets of the HDF5 file `h5_name`
+std::string post_xdmf(const tlbm_problem& p, const std::string& h5_name, bool time_avg);
 
-// writes <dir>/<stem>.bin (planes) and <dir>/<xmf>; returns false with *err on failure
-bool post_write(const std::string& dir, const std::string& bin_name, const std::string& xmf_name,
+// writeH5 / writeH5_time_avg (python/hdf5Helper.py:4-56): <dir>/<h5_name> with the planes above
+// as the groups and datasets processTLBM.py stores, and <dir>/<xmf_name>; false with *err on
+// failure
+bool post_write(const std::string& dir, const std::string& h5_name, const std::string& xmf_name,
                 const tlbm_problem& p, const float* planes, bool time_avg, std::string* err);
 
 }  // namespace tlbm

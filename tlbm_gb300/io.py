@@ -28,11 +28,25 @@ def read_dump(workdir: str, dump: int, dtype=np.float32, fields=("ux", "uy", "uz
     return out
 
 
-def create_restart(workdir: str, dump: int, out_dir: str | None = None, dtype=np.float32):
-    """Write restart_{ux,uy,uz,rho}.b_dat (float32, global order) from dump `dump`."""
+def create_restart(workdir: str, dump: int, out_dir: str | None = None, dtype=np.float32,
+                   fmt: str = "h5"):
+    """python/tLBM_create_restart.py: dump `dump` in global order as restart.h5
+    (velocity/{x,y,z}, density/rho, float32) -- or, with fmt="raw", as
+    restart_{ux,uy,uz,rho}.b_dat."""
+    from . import h5
+
     out_dir = out_dir or workdir
     d = read_dump(workdir, dump, dtype)
     os.makedirs(out_dir, exist_ok=True)
+    if fmt == "h5":
+        path = os.path.join(out_dir, "restart.h5")
+        if os.path.exists(path):  # h5py.File(..., 'w-') refuses an existing file
+            raise FileExistsError(path)
+        h5.write(path, {"velocity/x": d["ux"].astype(np.float32),
+                        "velocity/y": d["uy"].astype(np.float32),
+                        "velocity/z": d["uz"].astype(np.float32),
+                        "density/rho": d["density"].astype(np.float32)})
+        return out_dir
     for src, dst in (("ux", "ux"), ("uy", "uy"), ("uz", "uz"), ("density", "rho")):
         d[src].astype(np.float32).tofile(os.path.join(out_dir, "restart_%s.b_dat" % dst))
     return out_dir
