@@ -121,3 +121,27 @@ def test_unsupported_layouts_are_reported(harness, tmp_path):
     with pytest.raises(ValueError, match="not an HDF5 file"):
         open(g, "wb").write(b"plain text, not HDF5 at all" * 4)
         cpp_read(harness, g, "x")
+
+
+def _library_file():
+    """An HDF5 file written by the HDF5 library itself (MATLAB 7.3 format: a 512-byte user
+    block, superblock 0, a version-2 layout message, float64 data), shipped with scipy's test
+    data; its dataset testdouble holds 0, pi/4, ..., 2 pi as a 9 x 1 array."""
+    try:
+        import scipy.io.matlab as m
+    except ImportError:
+        return None
+    path = os.path.join(os.path.dirname(m.__file__), "tests", "data", "testhdf5_7.4_GLNX86.mat")
+    return path if os.path.exists(path) else None
+
+
+def test_readers_read_a_file_written_by_the_hdf5_library(harness):
+    path = _library_file()
+    if path is None:
+        pytest.skip("scipy's HDF5-based MAT test file is not installed")
+    want = np.arange(9) * np.pi / 4
+    a = h5.read(path, "testdouble")
+    assert a.dtype == np.float64 and a.shape == (9, 1)
+    assert np.allclose(a.reshape(-1), want, rtol=1e-15, atol=1e-15)
+    b = cpp_read(harness, path, "testdouble")
+    assert b.shape == (9, 1) and np.array_equal(b, a.astype(np.float32))

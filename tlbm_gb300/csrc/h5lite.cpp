@@ -533,10 +533,13 @@ std::string read_f32(const std::string& file, const std::string& path, std::vect
   r.f.open(file, std::ios::binary | std::ios::ate);
   if (!r.f.is_open()) return "cannot open " + file;
   r.size = static_cast<uint64_t>(r.f.tellg());
+  // the superblock sits at 0 or, after a user block, at 512, 1024, 2048, ...
   std::vector<uint8_t> sb;
-  if (!r.bytes(0, std::min<uint64_t>(r.size, 100), &sb) || sb.size() < 48 ||
-      std::memcmp(sb.data(), "\x89HDF\r\n\x1a\n", 8) != 0)
-    return file + " is not an HDF5 file";
+  for (uint64_t at = 0;; at = at == 0 ? 512 : 2 * at) {
+    if (at + 48 > r.size) return file + " is not an HDF5 file";
+    if (!r.bytes(at, std::min<uint64_t>(r.size - at, 100), &sb)) return file + ": " + r.err;
+    if (std::memcmp(sb.data(), "\x89HDF\r\n\x1a\n", 8) == 0) break;
+  }
   uint64_t root = kUndef;
   const unsigned ver = sb[8];
   if (ver == 0 || ver == 1) {

@@ -268,18 +268,23 @@ def read(path, name):
     """Dataset ``name`` (``"group/name"``) of the HDF5 file at ``path`` as a numpy array of its
     stored type (float32 or float64) and shape."""
     f = _File(path)
-    if f.b[:8] != SIGNATURE:
-        raise ValueError("%s is not an HDF5 file" % path)
-    ver = f.b[8]
+    # the superblock sits at 0 or, after a user block, at 512, 1024, 2048, ...
+    sb = 0
+    while f.b[sb:sb + 8] != SIGNATURE:
+        sb = 512 if sb == 0 else 2 * sb
+        if sb + 8 > len(f.b):
+            raise ValueError("%s is not an HDF5 file" % path)
+    s = f.b[sb:sb + 100]
+    ver = s[8]
     if ver in (0, 1):
-        if f.b[13] != 8 or f.b[14] != 8:
+        if s[13] != 8 or s[14] != 8:
             raise ValueError("only 8-byte offsets and lengths are read")
         b = 24 if ver == 0 else 28
-        f.base = _u(f.b, b, 8)
-        obj = _u(f.b, b + 40, 8)
+        f.base = _u(s, b, 8)
+        obj = _u(s, b + 40, 8)
     elif ver in (2, 3):
-        f.base = _u(f.b, 12, 8)
-        obj = _u(f.b, 36, 8)
+        f.base = _u(s, 12, 8)
+        obj = _u(s, 36, 8)
     else:
         raise ValueError("unknown superblock version %d" % ver)
     for part in [p for p in name.split("/") if p]:
