@@ -138,6 +138,8 @@ def test_closure_pipeline_small():
                        snap_every=32, train_from=96, epochs=15)
     print(out)
     assert out["fine_finite"]
+    # the fine run's collision is reported, with its departure from plain BGK
+    assert out["fine_run"]["collision"] == "smagorinsky" and out["fine_run"]["deviation"]
     assert out["loss_final"] < out["loss_initial"]
     assert out["learned"]["finite"] and out["smagorinsky"]["finite"]
 

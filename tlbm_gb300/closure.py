@@ -309,6 +309,13 @@ def study(cx=128, cy=64, cz=64, factor=4, u_in=0.05, re=3000.0, noise_amp=0.01,
     smag_cs = min((fl for fl in floors if fl > 0), key=lambda fl: scores[(fl, 0.0)])
     out = {"samples": int(len(nut)), "nu_t_mean": float(nut.mean()), "nu": nu_c,
            "fine_finite": bool(np.isfinite(ref).all()),
+           # the fine run is specified as plain BGK; at this Re and resolution BGK diverges
+           # (fine tau 0.5128), so unless fine_cs = 0 it relaxes with a constant Smagorinsky cs
+           "fine_run": {"collision": "smagorinsky" if fine_cs > 0 else "bgk",
+                        "cs": fine_cs, "factor": factor,
+                        "deviation": ("plain BGK specified; constant Smagorinsky cs = %g used "
+                                      "because BGK diverges at this resolution" % fine_cs)
+                        if fine_cs > 0 else None},
            "loss_initial": float(cl["loss_initial"]), "loss_final": float(cl["losses"][-1]),
            "calibration": {"step": calib_step, "floor_cs": floor, "multiplier": mult,
                            "smagorinsky_cs": smag_cs,
