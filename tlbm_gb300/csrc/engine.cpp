@@ -548,7 +548,6 @@ Status Engine::init(const int32_t* nd_type, const int32_t* parts, int size) {
     }
     TLBM_TRY(load_restart(r[0].data(), r[1].data(), r[2].data(), r[3].data()));
   }
-  TLBM_CUDA(cudaMallocHost(&h_pinned_, n * std::max(ob_, 4)));
 
   // write_node_ordering (src/TLBM_Partition.cpp:542-561)
   if (!workdir_.empty()) {
@@ -746,6 +745,10 @@ Status Engine::fetch(const void* dev, void* host) {
 }
 
 Status Engine::write_field(const std::string& name, const void* dev) {
+  // the page-locked staging buffer of the dump files, made at the first dump (pinning a field's
+  // worth of host memory takes tens of milliseconds; runs without file dumps never pay it)
+  if (!h_pinned_)
+    TLBM_CUDA(cudaMallocHost(&h_pinned_, static_cast<size_t>(n_) * std::max(ob_, 4)));
   TLBM_TRY(fetch(dev, h_pinned_));
   return write_at(workdir_ + "/" + name, h_pinned_, static_cast<size_t>(n_) * ob_, 0);
 }
