@@ -1,8 +1,8 @@
 """The fixed-point FP64-storage collision (tlbm_gb300/csrc/physics_fx.cuh) compiled for the host:
 random near-equilibrium cells collided by it and by a long-double evaluation of the reference's
 formulas (moments, equilibrium with the reference's weights, Smagorinsky rate, BGK relaxation)
-differ by at most 3 ulp of the result (2 ulp on D3Q19; the 3 ulp are D3Q27's smallest
-populations, ~0.002, where one ulp is 4e-19), and most results are the nearest double.  The exact
+differ by at most 3 ulp of the result (2 ulp on D3Q19; the 3 ulp are the smallest D3Q15 and
+D3Q27 populations, ~0.002, where one ulp is 4e-19), and most results are the nearest double.  The exact
 double <-> fixed-point conversions, the integer reciprocal and the range guards are checked
 too."""
 
