@@ -527,6 +527,43 @@ def test_fast_wrap_on_degenerate_lattices(q, dims, arith):
     assert rel_inf(fast[3], ref[3]) <= 1e-12
 
 
+@pytest.mark.parametrize("q", [19, 27])
+def test_fast_fp64_force_and_closure_on_fixed_point_storage(q):
+    """The paths around the fixed-point step that read FP64 populations held as Q1.62: the
+    momentum-exchange force against the reference-arithmetic kernel (within 1e-12 of the
+    largest force component), and the learned-closure step (its own kernel, FP64 code on the
+    converted populations) against the same closure on IEEE-double storage (f64_pipe)."""
+    g, p = sphere_pack_slab(q, nx=64, ny=32, nz=48, seed=3)
+    out = {}
+    for a in ("reference", "fast"):
+        part = T.TLBMPartition.from_arrays(T.problem_from_params(p), g.nd_type, precision="f64",
+                                           arithmetic=a)
+        part.run(0, 60)
+        out[a] = part.force()
+        part.close()
+    scale = max(float(np.abs(f).max()) for f in out["reference"])
+    assert scale > 0
+    for a, b in zip(out["fast"], out["reference"]):
+        assert np.abs(a - b).max() <= 1e-12 * scale
+    from tlbm_gb300 import mlp_params
+
+    nu = (1.0 / p.omega - 0.5) / 3.0
+    mac = []
+    for a in FAST64:
+        part = T.TLBMPartition.from_arrays(T.problem_from_params(p), g.nd_type, precision="f64",
+                                           arithmetic=a)
+        part.set_closure_mlp(mlp_params.xavier(3), np.ones(8), np.zeros(8), 1e-4,
+                             3.0 * nu + 0.5 + 1e-6)
+        part.run(0, 40)
+        mac.append(part.macros())
+        part.close()
+    u_scale = max(float(np.abs(m).max()) for m in mac[1][:3])
+    for k in range(4):
+        sc = u_scale if k < 3 else float(np.abs(mac[1][3]).max())
+        assert np.all(np.isfinite(mac[0][k]))
+        assert np.abs(mac[0][k] - mac[1][k]).max() <= 1e-12 * sc, k
+
+
 def _pairs_case(name, q):
     """Lattices for the x-pair 16-bit step: the sphere-pack slab (fluid, solid, inlet and
     outlet planes), the lid cavity (type-5 lid) and periodic boxes of random fluid/solid nodes
