@@ -297,6 +297,26 @@ def cpu_baseline(g, p, seconds=10.0, chunk=10, warmup=2):
     }
 
 
+def config_of(args, g, p, dist):
+    """The workload both arms report: the sphere pack, its flow and its memory footprint."""
+    n = g.num_nodes
+    q = int(args.lattice[3:])
+    return {
+        "workload": "%dx%dx%d sphere-packed channel, %s BGK+Smagorinsky cs=0.1, %s %s "
+                    "arithmetic" % (args.nx, args.ny, args.nz, args.lattice, args.precision,
+                                    args.arithmetic),
+        "cells": n,
+        "porosity": round(g.meta.get("porosity", 0.0), 5),
+        "spheres": g.meta.get("n_spheres"),
+        "re": 200.0,
+        "u_in": 0.04,
+        "omega": round(p.omega, 6),
+        "l2": "populations (%.1f GB) larger than L2; no flush" % (
+            n * (cell_bytes(q, args.precision) - 1) / 1e9),
+        "parallelism": "replicas only" if dist.world > 1 else "single GPU",
+    }
+
+
 def run_ours(args, dist):
     import tlbm_gb300 as T
     from tlbm_gb300 import build as B
@@ -347,20 +367,7 @@ def run_ours(args, dist):
                   "bf16-moment-shifted-storage/f32", "f16":
                   "f16-storage/f32"}[args.precision],
         "data": "synthetic",
-        "config": {
-            "workload": "%dx%dx%d sphere-packed channel, %s BGK+Smagorinsky cs=0.1, %s %s "
-                        "arithmetic" % (args.nx, args.ny, args.nz, args.lattice, args.precision,
-                                        args.arithmetic),
-            "cells": n,
-            "porosity": round(g.meta.get("porosity", 0.0), 5),
-            "spheres": g.meta.get("n_spheres"),
-            "re": 200.0,
-            "u_in": 0.04,
-            "omega": round(p.omega, 6),
-            "l2": "populations (%.1f GB) larger than L2; no flush" % (
-                n * (cell_bytes(q, args.precision) - 1) / 1e9),
-            "parallelism": "replicas only" if dist.world > 1 else "single GPU",
-        },
+        "config": config_of(args, g, p, dist),
         "roofline": {
             "bound": "hbm",
             "achieved": round(achieved, 1),
@@ -568,46 +575,51 @@ def e2e(args, g, p, dist, plot_every=100):
     }
 
 
-def run_reference(args, dist):
-    """The reference's CPU timestep on all host cores: its C restatement in oracle/, pinned
+def run_reference(args, dist, budget_s=60.0):
+    """The reference's CPU timestep on all host cores, on the whole workload: its C restatement
+    in oracle/ (AoS push through an int32 neighbour table, OpenMP over nodes), pinned
     byte-identical to the reference's own build.  That build (oracle/_ref, compiled from the
     reference's sources where they exist) is built for the machine that compiled it; a machine
-    of another architecture without those sources can neither run nor rebuild it."""
+    of another architecture without those sources can neither run nor rebuild it.  The timed
+    steps are the requested ones, or as many as fit `budget_s` seconds at the rate of the
+    warm-up steps (a bounded sample of the same run)."""
     g, p = workload(args)
     sys.path.insert(0, os.path.join(HERE, "tests"))
     import oracle_lib
 
-    nd, nz = cpu_sample(g, p)
     q = int(args.lattice[3:])
     threads = os.cpu_count() or 1
-    o = oracle_lib.Oracle(q, 1, p.cs, p.rho_lbm, p.u_lbm, p.omega, g.nx, g.ny, nz, nd,
+    o = oracle_lib.Oracle(q, 1, p.cs, p.rho_lbm, p.u_lbm, p.omega, g.nx, g.ny, g.nz, g.nd_type,
                           prec="f64", threads=threads)
-    o.run(args.warmup)
+    warm = min(args.warmup, 3)
     t0 = time.perf_counter()
-    o.run(args.steps)
+    o.run(warm)
+    per_step = (time.perf_counter() - t0) / warm
+    steps = max(1, min(args.steps, int(budget_s / max(per_step, 1e-9))))
+    t0 = time.perf_counter()
+    o.run(steps)
     dt = time.perf_counter() - t0
     o.close()
-    cells = g.nx * g.ny * nz
-    value = cells * args.steps / dt / 1e6
-    sample = ("%dx%dx%d slab of the %dx%dx%d sphere pack per step, FP64 BGK+Smagorinsky, C "
-              "restatement of the reference timestep, OpenMP over nodes"
-              % (g.nx, g.ny, nz, g.nx, g.ny, g.nz))
+    cells = g.num_nodes
+    value = cells * steps / dt / 1e6
+    sample = ("the whole %dx%dx%d sphere pack, FP64 BGK+Smagorinsky, %d warm-up + %d timed steps "
+              "(%.1f s) of the C restatement of the reference timestep, OpenMP over nodes"
+              % (g.nx, g.ny, g.nz, warm, steps, dt))
     return {
         "impl": "reference",
         "metric": METRIC,
         "value": round(value, 3),
         "unit": "MLUPS",
         "n_gpus": dist.world,
-        "steps": args.steps,
-        "warmup": args.warmup,
-        "ms_per_step": round(dt * 1e3 / args.steps, 3),
+        "steps": steps,
+        "warmup": warm,
+        "ms_per_step": round(dt * 1e3 / steps, 3),
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": "%dx%dx%d sphere-packed channel, %s BGK+Smagorinsky cs=0.1, f64"
-                               % (args.nx, args.ny, args.nz, args.lattice)},
+        "config": config_of(args, g, p, dist),
         "cpu_baseline": {"value": round(value, 3), "unit": "MLUPS", "cores": threads,
                          "kind": "port", "sample": sample},
         "e2e": {"value": round(value, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0,
