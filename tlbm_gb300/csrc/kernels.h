@@ -45,7 +45,6 @@ struct StepArgs {
   int time_avg;
   const void* uyq_cur;   // uy of nodes 0..Q-1 in this step   (type-5 quirk, see ref::set_uz)
   const void* uyq_prev;  // uy of nodes 0..Q-1 in the previous step
-  void* macro[4];        // fused macroscopic output (fast kernels; null when not wanted)
   const void* closure;   // learned closure (mlp::Closure in HOST memory; the launch copies it
                          // into the kernel's parameters) or null
 };
