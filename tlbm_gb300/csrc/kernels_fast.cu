@@ -88,6 +88,17 @@ __global__ void __launch_bounds__(128, kFxMinBlocks<L>)
   cell_step_fx<L, K, kClosure>(a, x, y, z);
 }
 
+// Q1.62 storage, plane bases in the parameters (step_fast.cuh: cell_step_fxp)
+template <class L, int kClosure>
+__global__ void __launch_bounds__(128, kFxMinBlocks<L>)
+    k_step_fast_fxp(const __grid_constant__ FxArgs fa) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= fa.a.pb.nx || y >= fa.a.pb.ny) return;
+  cell_step_fxp<L, kClosure>(fa, x, y, z);
+}
+
 // an opaque copy: the compiler cannot reuse values computed from v before this point
 __device__ __forceinline__ void launder(float& v) { asm volatile("" : "+f"(v)); }
 __device__ __forceinline__ void launder(double& v) { asm volatile("" : "+d"(v)); }
@@ -298,7 +309,19 @@ cudaError_t step_lk(const StepArgs& a, const Launch& l) {
       k_step_fast_mlp<L, K, false><<<g, b, 0, l.stream>>>(a, cl);
   } else if ((K == kStoreF64 || K == kStoreFX) && a.pb.fx && !a.pb.mcoll) {
     // FP64 storage (double or Q1.62): fluid nodes in exact fixed point (physics_fx.cuh)
-    if constexpr (K == kStoreF64 || K == kStoreFX) {
+    if constexpr (K == kStoreFX) {
+      FxArgs fa{};
+      fa.a = a;
+      const size_t n = static_cast<size_t>(a.pb.n);
+      for (int i = 0; i < L::Q; ++i) {
+        fa.src[i] = static_cast<const fx::i64*>(a.src) + i * n;
+        fa.dst[i] = static_cast<fx::i64*>(a.dst) + i * n;
+      }
+      if (a.pb.cs > 0)
+        k_step_fast_fxp<L, fast::kClosureSmag><<<g, b, 0, l.stream>>>(fa);
+      else
+        k_step_fast_fxp<L, fast::kClosureNone><<<g, b, 0, l.stream>>>(fa);
+    } else if constexpr (K == kStoreF64) {
       if (a.pb.cs > 0)
         k_step_fast_fx<L, K, fast::kClosureSmag><<<g, b, 0, l.stream>>>(a);
       else

@@ -103,8 +103,9 @@ __device__ __forceinline__ void load_raw(const StepArgs& a, int x, int y, int z,
       const float4* prm = moment::params(a.src, L::Q, static_cast<size_t>(pb.n)) + c;
 #pragma unroll
       for (int i = 0; i < L::Q; ++i)
-        raw[i] = __fadd_rn(moment::shift<L>(i, __ldg(prm - pb.pull_cell[i])),
-                           __bfloat162float(__ldg(reinterpret_cast<const P*>(base + pb.pull_off[i]))));
+        raw[i] = __fadd_rn(
+            moment::shift<L>(i, __ldg(prm - pb.pull_cell[i])),
+            __bfloat162float(__ldg(reinterpret_cast<const P*>(base + pb.pull_off[i]))));
     } else {
 #pragma unroll
       for (int i = 0; i < L::Q; ++i)
@@ -263,6 +264,56 @@ __device__ __forceinline__ void cell_step_fx(const StepArgs& a, int x, int y, in
     }
   }
   cell_step_f64_cold<L, K, kClosure>(a, x, y, z);
+}
+
+// The same step for Q1.62 storage with each population plane's first element in the kernel
+// parameters (as the x-pair step): a load or store address is one multiply-add of a 32-bit cell
+// index onto a parameter, where the one-buffer form adds a 64-bit byte offset per speed.
+struct FxArgs {
+  StepArgs a;
+  const fx::i64* src[27];
+  fx::i64* dst[27];
+};
+
+template <class L, int kClosure>
+__device__ __forceinline__ void cell_step_fxp(const FxArgs& fa, int x, int y, int z) {
+  const StepArgs& a = fa.a;
+  const DevProblem& pb = a.pb;
+  const int c = x + y * pb.nx + z * pb.nxy;
+  fx::i64 f[L::Q];
+  if (z > 0 && z < pb.nz - 1) {
+    // speed i pulls from c - e_i; across an x or y edge from the far side of the plane
+    const int wx_pos = x == 0 ? pb.nx : 0, wx_neg = x == pb.nx - 1 ? -pb.nx : 0;
+    const int wy_pos = y == 0 ? pb.nxy : 0, wy_neg = y == pb.ny - 1 ? -pb.nxy : 0;
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) {
+      const int ex = L::ex(i), ey = L::ey(i);
+      const int w = (ex > 0 ? wx_pos : (ex < 0 ? wx_neg : 0)) +
+                    (ey > 0 ? wy_pos : (ey < 0 ? wy_neg : 0));
+      f[i] = __ldg(fa.src[i] + static_cast<unsigned>(c - pb.pull_cell[i] + w));
+    }
+  } else {
+    const Nbr nb(x, y, z, pb.nx, pb.ny, pb.nz, pb.nxy);
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) f[i] = __ldg(fa.src[i] + static_cast<unsigned>(nb.from<L>(i)));
+  }
+  const uint8_t t = pb.nd_type[c];
+  if (!a.time_avg && pb.fx) {
+    const unsigned cu = static_cast<unsigned>(c);
+    if (t == kSolid) {
+#pragma unroll
+      for (int i = 0; i < L::Q; ++i) fa.dst[i][cu] = f[L::bb(i)];
+      return;
+    }
+    fx::i64 rq, jq[3];
+    if (t == kFluid && relaxes(pb) &&
+        fx::fluid_collide<L, kClosure == fast::kClosureSmag>(f, pb.fxk, rq, jq)) {
+#pragma unroll
+      for (int i = 0; i < L::Q; ++i) fa.dst[i][cu] = f[i];
+      return;
+    }
+  }
+  cell_step_f64_cold<L, kStoreFX, kClosure>(a, x, y, z);
 }
 
 // the part of cell_step after the loads: node-type branch, collision, store
