@@ -145,3 +145,58 @@ def test_readers_read_a_file_written_by_the_hdf5_library(harness):
     assert np.allclose(a.reshape(-1), want, rtol=1e-15, atol=1e-15)
     b = cpp_read(harness, path, "testdouble")
     assert b.shape == (9, 1) and np.array_equal(b, a.astype(np.float32))
+
+
+def _v2_file(path):
+    """A file in HDF5's newer layouts, assembled by hand from the specification: superblock
+    version 2, version-2 object headers ("OHDR", with a continuation chunk "OCHK"), a root group
+    held as link messages, version-2 dataspaces, and one compact and one contiguous float32
+    dataset.  Checksums are left zero (neither reader verifies them)."""
+    img = bytearray(48)  # superblock, written last
+
+    def put(b):
+        at = len(img)
+        img.extend(b)
+        return at
+
+    def ohdr(messages):
+        body = b"".join(struct.pack("<BHB", t, len(d), 0) + d for t, d in messages)
+        return b"OHDR" + struct.pack("<BBI", 2, 2, len(body)) + body + b"\0" * 4
+
+    space = lambda dims: struct.pack("<BBBB", 2, len(dims), 0, 1) + b"".join(
+        struct.pack("<Q", d) for d in dims)
+    f32 = struct.pack("<BBBBIHHBBBBI", 0x11, 0x20, 31, 0, 4, 0, 32, 23, 8, 0, 23, 127)
+    small = np.array([1.5, -2.25, 3.0], np.float32)
+    big = np.arange(12, dtype=np.float32).reshape(3, 4) / 4
+    compact = ohdr([(1, space([3])), (3, f32),
+                    (8, struct.pack("<BBH", 3, 0, small.nbytes) + small.tobytes())])
+    a_small = put(compact)
+    data = put(big.tobytes())
+    a_big = put(ohdr([(1, space([3, 4])), (3, f32),
+                      (8, struct.pack("<BBQQ", 3, 1, data, big.nbytes))]))
+
+    def link(name, addr):
+        return (6, struct.pack("<BBB", 1, 0, len(name)) + name.encode() + struct.pack("<Q", addr))
+
+    cont = [link("big", a_big)]
+    cbody = b"".join(struct.pack("<BHB", t, len(d), 0) + d for t, d in cont)
+    a_chunk = put(b"OCHK" + cbody + b"\0" * 4)
+    root = put(ohdr([link("small", a_small),
+                     (0x10, struct.pack("<QQ", a_chunk, 4 + len(cbody) + 4))]))
+    sb = b"\x89HDF\r\n\x1a\n" + struct.pack("<BBBB", 2, 8, 8, 0)
+    sb += struct.pack("<QQQQ", 0, h5.UNDEF, len(img), root) + b"\0" * 4
+    img[0:48] = sb
+    open(path, "wb").write(bytes(img))
+    return small, big
+
+
+def test_readers_take_newer_layouts(harness, tmp_path):
+    f = str(tmp_path / "v2.h5")
+    small, big = _v2_file(f)
+    for name, want in (("small", small), ("big", big)):
+        a = h5.read(f, name)
+        assert a.shape == want.shape and np.array_equal(a, want), name
+        b = cpp_read(harness, f, name)
+        assert b.shape == want.shape and np.array_equal(b, want), name
+    with pytest.raises(KeyError):
+        h5.read(f, "missing")
