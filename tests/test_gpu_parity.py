@@ -564,6 +564,29 @@ def test_fast_fp64_force_and_closure_on_fixed_point_storage(q):
         assert np.abs(mac[0][k] - mac[1][k]).max() <= 1e-12 * sc, k
 
 
+@pytest.mark.parametrize("q", [19, 27])
+def test_fast_fp64_at_water_density_takes_double_storage(q):
+    """tLBM_write_params.py writes rhoLBM = rho_p l_conv^3 (1000 for water): populations of
+    that size are outside the Q1.62 range, so fast FP64 keeps IEEE-double storage and every
+    fluid node fails the fixed-point guards and takes the FP64 code -- the same numbers as the
+    FP64-arithmetic path, bit for bit, and within 1e-12 of the reference arithmetic."""
+    g, p = sphere_pack_slab(q, nx=32, ny=24, nz=40, seed=5)
+    p.rho_lbm = 1000.0
+    out = {}
+    for a in ("reference", "fast", "fast-fp64"):
+        part = T.TLBMPartition.from_arrays(T.problem_from_params(p), g.nd_type, precision="f64",
+                                           arithmetic=a)
+        part.run(0, 40)
+        out[a] = part.macros()
+        part.close()
+    for a, b in zip(out["fast"], out["fast-fp64"]):
+        assert np.array_equal(a, b)
+    u_scale = max(float(np.abs(m).max()) for m in out["reference"][:3])
+    for k in range(4):
+        sc = u_scale if k < 3 else float(np.abs(out["reference"][3]).max())
+        assert np.abs(out["fast"][k] - out["reference"][k]).max() <= 1e-12 * sc, k
+
+
 def _pairs_case(name, q):
     """Lattices for the x-pair 16-bit step: the sphere-pack slab (fluid, solid, inlet and
     outlet planes), the lid cavity (type-5 lid) and periodic boxes of random fluid/solid nodes
