@@ -13,6 +13,7 @@
 #include <cstdlib>
 #include <random>
 
+#include "../tlbm_gb300/csrc/grid.cuh"
 #include "../tlbm_gb300/csrc/physics_fx.cuh"
 
 using namespace tlbm;
@@ -261,6 +262,77 @@ void guards() {
   CHECK((fx::fluid_collide<L, false>(F, k, rq, jq)), "stored state at rest accepted");
 }
 
+// The output fields' helpers: the half-range test, Q5.58 rounding, the pair moments against
+// long-double sums, and the two-step neighbour offsets of the force terms against modular
+// arithmetic on small lattices (where the wraps interact).
+void output_helpers(unsigned seed) {
+  std::mt19937_64 rng(seed);
+  const fx::i64 half = 1LL << 61;
+  const fx::i64 edges[] = {0, 1, -1, half - 1, half, -half, -half + 1, -half - 1, fx::kStoreNaN,
+                           0x7FFFFFFFFFFFFFFFLL};
+  for (fx::i64 v : edges) {
+    const bool beyond = v >= half || v < -half;  // -1/2 <= f < 1/2 passes
+    CHECK((fx::beyond_half(v) != 0) == beyond, "beyond_half(%lld)", v);
+  }
+  for (int t = 0; t < 1000000; ++t) {
+    const fx::i64 v = static_cast<fx::i64>(rng()) >> (rng() % 64);
+    const bool beyond = v >= half || v < -half;
+    CHECK((fx::beyond_half(v) != 0) == beyond, "beyond_half(%lld)", v);
+    if (!beyond) {  // nearest multiple of 16 (ties up)
+      const fx::i64 r = fx::to58(v);
+      CHECK(r * 16 - v >= -7 && r * 16 - v <= 8, "to58(%lld) = %lld", v, r);
+    }
+    if (fails > 10) return;
+  }
+  // pair moments of random in-range states: each pair sum rounded once to 2^-59
+  std::uniform_real_distribution<double> U(-1.0, 1.0);
+  for (int t = 0; t < 100000; ++t) {
+    using L = Lattice<19>;
+    fx::i64 F[L::Q];
+    LD rho = 0, jx = 0, jy = 0, jz = 0;
+    for (int i = 0; i < L::Q; ++i) {
+      F[i] = static_cast<fx::i64>(std::ldexp(i == 0 ? 0.5 + 0.49 * U(rng) : 0.49 * U(rng), 62));
+      const LD v = std::ldexp(static_cast<LD>(F[i]), -62);
+      rho += v;
+      jx += L::ex(i) * v;
+      jy += L::ey(i) * v;
+      jz += L::ez(i) * v;
+    }
+    CHECK(fx::in_q62_ranges<L>(F), "in range");
+    fx::i64 r, x, y, z;
+    fx::pair_moments<L>(F, r, x, y, z);
+    const LD tol = 10 * 0x1p-60L;  // one 2^-60 rounding per pair and the rest population
+    CHECK(std::fabs(std::ldexp(static_cast<LD>(r), -59) - rho) <= tol, "rho");
+    CHECK(std::fabs(std::ldexp(static_cast<LD>(x), -59) - jx) <= tol, "jx");
+    CHECK(std::fabs(std::ldexp(static_cast<LD>(y), -59) - jy) <= tol, "jy");
+    CHECK(std::fabs(std::ldexp(static_cast<LD>(z), -59) - jz) <= tol, "jz");
+    CHECK(fx::to_f64_58(x) == std::ldexp(fx::to_f64_59(x), 1), "Q5.58 scaling");
+    if (fails > 10) return;
+  }
+  const int sizes[] = {1, 2, 3, 5};
+  for (int nx : sizes)
+    for (int ny : sizes)
+      for (int nz : sizes) {
+        const int nxy = nx * ny;
+        for (int zz = 0; zz < nz; ++zz)
+          for (int yy = 0; yy < ny; ++yy)
+            for (int xx = 0; xx < nx; ++xx) {
+              const Nbr nb(xx, yy, zz, nx, ny, nz, nxy);
+              const Nbr2 n2(nb, nx, ny, nz, nxy);
+              for (int i = 0; i < 27; ++i) {
+                using L = Lattice<27>;
+                const int wx = ((xx + 2 * L::ex(i)) % nx + nx) % nx;
+                const int wy = ((yy + 2 * L::ey(i)) % ny + ny) % ny;
+                const int wz = ((zz + 2 * L::ez(i)) % nz + nz) % nz;
+                CHECK(n2.to2<L>(nb, i) == wx + wy * nx + wz * nxy, "c + 2e_%d at (%d %d %d) of "
+                      "%dx%dx%d", i, xx, yy, zz, nx, ny, nz);
+              }
+            }
+        if (fails > 10) return;
+      }
+  std::printf("output helpers: checked\n");
+}
+
 int main(int argc, char** argv) {
   const int q = argc > 1 ? std::atoi(argv[1]) : 19;
   const bool smag = argc > 2 && std::atoi(argv[2]) != 0;
@@ -268,6 +340,7 @@ int main(int argc, char** argv) {
   const unsigned seed = argc > 4 ? static_cast<unsigned>(std::atoi(argv[4])) : 1u;
   if (q == 0) {
     conversions(seed);
+    output_helpers(seed);
     guards<Lattice<15>>();
     guards<Lattice<19>>();
     guards<Lattice<27>>();

@@ -4,7 +4,8 @@ formulas (moments, equilibrium with the reference's weights, Smagorinsky rate, B
 differ by at most 3 ulp of the result (2 ulp on D3Q19; the 3 ulp are the smallest D3Q15 and
 D3Q27 populations, ~0.002, where one ulp is 4e-19), and most results are the nearest double.  The exact
 double <-> fixed-point conversions, the integer reciprocal and the range guards are checked
-too."""
+too, and so are the output fields' helpers: the pair moments, the Q5.58 rounding of the force
+sums and the two-step neighbour offsets of the force terms."""
 
 import os
 import re

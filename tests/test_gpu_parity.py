@@ -82,7 +82,7 @@ def test_tlbmexec_cli_fp32_bit_exact(tmp_path):
 FAST64 = ["fast", "fast-fp64"]
 
 
-def fast_vs_reference(name, prec, tmp_path, steps=None, arith="fast"):
+def fast_vs_reference(name, prec, tmp_path, steps=None, arith="fast", what="macros"):
     spec = CASES[name]["spec"]
     d_ref = os.path.join(str(tmp_path), "ref")
     d_fast = os.path.join(str(tmp_path), "fast")
@@ -93,7 +93,7 @@ def fast_vs_reference(name, prec, tmp_path, steps=None, arith="fast"):
     for d, p, a in ((d_ref, "f64", "reference"), (d_fast, prec, arith)):
         part = T.TLBMPartition(d, precision=p, arithmetic=a)
         part.run(0, steps)
-        out.append(part.macros())
+        out.append(getattr(part, what)())
         part.close()
     return out
 
@@ -104,6 +104,20 @@ def test_fast_fp64_channel32_2000_within_1e12(arith, tmp_path):
     errs = [rel_inf(a, b) for a, b in zip(fast, ref)]
     print("channel 32x32x128, 2000 steps, %s: rel_inf ux %.2e uy %.2e uz %.2e rho %.2e"
           % (arith, *errs))
+    assert max(errs) <= 1e-12, errs
+
+
+@pytest.mark.parametrize("arith", FAST64)
+@pytest.mark.parametrize("name,steps", [("channel32_q19_2000", None), ("q27_sphere_smag", 150),
+                                        ("q15_sphere_smag", 150)])
+def test_fast_fp64_force_within_1e12(name, steps, arith, tmp_path):
+    """calc_force (src/TLBM_Partition.cpp:174-208) in fast arithmetic against the
+    reference-arithmetic kernel: Q1.62 storage sums each boundary link's populations as
+    integers (one conversion per component), double storage in FP64."""
+    ref, fast = fast_vs_reference(name, "f64", tmp_path, steps=steps, arith=arith, what="force")
+    assert max(np.abs(r).max() for r in ref) > 1e-4  # the obstacle carries a force
+    errs = [rel_inf(a, b) for a, b in zip(fast, ref)]
+    print("%s, %s: force rel_inf Fx %.2e Fy %.2e Fz %.2e" % (name, arith, *errs))
     assert max(errs) <= 1e-12, errs
 
 

@@ -136,6 +136,27 @@ struct Nbr {
   }
 };
 
+// Cell c + 2 e_i (wrapped) from a cell's neighbour offsets: where the fluid neighbour
+// g = c + e_i pulls speed bb(i) from (the second source of a boundary link's force term).
+struct Nbr2 {
+  int xpp, xmm, ypp, ymm, zpp, zmm;  // x+2, x-2, row offsets of y+2, y-2, plane offsets z+-2
+
+  TLBM_HD Nbr2(const Nbr& b, int nx, int ny, int nz, int nxy) {
+    xpp = (b.xp == nx - 1) ? 0 : b.xp + 1;
+    xmm = (b.xm == 0) ? nx - 1 : b.xm - 1;
+    ypp = (b.yp == (ny - 1) * nx) ? 0 : b.yp + nx;
+    ymm = (b.ym == 0) ? (ny - 1) * nx : b.ym - nx;
+    zpp = (b.zp == (nz - 1) * nxy) ? 0 : b.zp + nxy;
+    zmm = (b.zm == 0) ? (nz - 1) * nxy : b.zm - nxy;
+  }
+  template <class L>
+  TLBM_HD int to2(const Nbr& b, int i) const {
+    const int ex = L::ex(i), ey = L::ey(i), ez = L::ez(i);
+    return (ex > 0 ? xpp : (ex < 0 ? xmm : b.x0)) + (ey > 0 ? ypp : (ey < 0 ? ymm : b.y0)) +
+           (ez > 0 ? zpp : (ez < 0 ? zmm : b.z0));
+  }
+};
+
 // cell index -> (x, y, z)
 TLBM_HD void decompose(int c, int nx, int nxy, int& x, int& y, int& z) {
   z = c / nxy;

@@ -218,11 +218,32 @@ __global__ void __launch_bounds__(128) k_macros_fast(DevProblem pb,
   const int c = nb.self();
   typename Store<K>::T raw[L::Q];
   load_cell<L, K>(src, static_cast<size_t>(pb.n), nb, raw);
+  const uint8_t t = pb.nd_type[c];
+  if constexpr (K == kStoreFX) {
+    // Q1.62 populations within the collision's ranges: density and momentum as its exact
+    // integer pair sums, so a node costs four conversions to double and the division instead
+    // of Q conversions and the FP64 sums; inlet and outlet nodes and states outside the
+    // ranges (the stored NaN included) take the FP64 code below
+    fx::i64 rq, jx, jy, jz;
+    if (t != kInlet && t != kOutlet && fx::in_q62_ranges<L>(raw)) {
+      fx::pair_moments<L>(raw, rq, jx, jy, jz);
+      const double rho = fx::to_f64_59(rq);
+      rho_o[c] = rho;
+      if (t == kSolid) {
+        ux_o[c] = uy_o[c] = uz_o[c] = 0.0;
+      } else {
+        const double inv = 1.0 / rho;
+        ux_o[c] = fx::to_f64_59(jx) * inv;
+        uy_o[c] = fx::to_f64_59(jy) * inv;
+        uz_o[c] = fx::to_f64_59(jz) * inv;
+      }
+      return;
+    }
+  }
   C f[L::Q];
   unpack<L, K>(raw, f);
   C rho, ux, uy, uz;
-  node_macros<L, C>(pb.nd_type[c], f, Par<C>::u_in(pb, c % pb.nxy), Par<C>::rho_bc(pb), rho, ux,
-                    uy, uz);
+  node_macros<L, C>(t, f, Par<C>::u_in(pb, c % pb.nxy), Par<C>::rho_bc(pb), rho, ux, uy, uz);
   ux_o[c] = ux;
   uy_o[c] = uy;
   uz_o[c] = uz;
@@ -248,20 +269,17 @@ __global__ void k_quirk_fast(DevProblem pb, const void* __restrict__ src,
   uy_out[c] = uy;
 }
 
+// The boundary-link sums of calc_force (src/TLBM_Partition.cpp:174-208) for solid node c, in the
+// storage kind's arithmetic: the fluid neighbour g = c + e_i adds (f_i arriving at c + f_bb(i)
+// arriving at g) e_bb(i), i.e. the stored values of speed i at c - e_i and of speed bb(i) at
+// c + 2 e_i.
 template <class L, int K>
-__global__ void __launch_bounds__(128) k_force_fast(DevProblem pb,
-                                                   const void* __restrict__ fv,
-                                                   typename Store<K>::C* fx_o,
-                                                   typename Store<K>::C* fy_o,
-                                                   typename Store<K>::C* fz_o) {
+__device__ __forceinline__ void force_links(const DevProblem& pb, const void* __restrict__ fv,
+                                            const Nbr& nb, const Nbr2& n2,
+                                            typename Store<K>::C& fx, typename Store<K>::C& fy,
+                                            typename Store<K>::C& fz) {
   using S = Store<K>;
   using C = typename S::C;
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  const int z = blockIdx.z;
-  if (x >= pb.nx || y >= pb.ny) return;
-  const Nbr nb(x, y, z, pb.nx, pb.ny, pb.nz, pb.nxy);
-  const int c = nb.self();
   const size_t n = static_cast<size_t>(pb.n);
   const auto* f = static_cast<const typename S::P*>(fv);
   // post-stream value of speed i at cell d: the slot (i, from) of the buffer
@@ -271,22 +289,89 @@ __global__ void __launch_bounds__(128) k_force_fast(DevProblem pb,
     else
       return S::load(f[i * n + from], fast::wgt<L, C>(i));
   };
-  C fx = 0, fy = 0, fz = 0;
-  if (pb.nd_type[c] == kSolid) {
 #pragma unroll
-    for (int i = 0; i < L::Q; ++i) {
-      const int g = nb.to<L>(i);
-      if (pb.nd_type[g] != kFluid) continue;
+  for (int i = 0; i < L::Q; ++i) {
+    if (pb.nd_type[nb.to<L>(i)] != kFluid) continue;
+    const int b = L::bb(i);
+    const C s = pulled(i, nb.from<L>(i)) + pulled(b, n2.to2<L>(nb, i));
+    fx += C(L::ex(b)) * s;
+    fy += C(L::ey(b)) * s;
+    fz += C(L::ez(b)) * s;
+  }
+}
+
+template <class L, int K>
+__global__ void __launch_bounds__(128) k_force_fast(DevProblem pb,
+                                                   const void* __restrict__ fv,
+                                                   typename Store<K>::C* fx_o,
+                                                   typename Store<K>::C* fy_o,
+                                                   typename Store<K>::C* fz_o) {
+  using C = typename Store<K>::C;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= pb.nx || y >= pb.ny) return;
+  const Nbr nb(x, y, z, pb.nx, pb.ny, pb.nz, pb.nxy);
+  const int c = nb.self();
+  C fx = 0, fy = 0, fz = 0;
+  if (pb.nd_type[c] == kSolid)
+    force_links<L, K>(pb, fv, nb, Nbr2(nb, pb.nx, pb.ny, pb.nz, pb.nxy), fx, fy, fz);
+  fx_o[c] = fx;
+  fy_o[c] = fy;
+  fz_o[c] = fz;
+}
+
+// the FP64 sums for a Q1.62 node the integer sums do not take (out of line: rare, and kept out
+// of the integer kernel's register allocation)
+template <class L>
+__device__ __noinline__ void force_links_f64(const DevProblem& pb, const void* fv, const Nbr& nb,
+                                             const Nbr2& n2, double& fx, double& fy, double& fz) {
+  force_links<L, kStoreFX>(pb, fv, nb, n2, fx, fy, fz);
+}
+
+// Q1.62 storage: the link sums accumulate as integers (each value rounded once to 2^-58; Q5.58
+// holds the 2 (Q - 1) values in [-1/2, 1/2) a node can gather), three conversions per node.  The
+// work sits in the warps that hold solid surface nodes and is bound by load latency: 64 registers
+// (eight resident blocks per SM, against three at the 138 the FP64 form of the sums takes) and
+// predicated loads that issue without waiting on each link's type test.  A value outside the
+// range (the stored NaN included) sends the node to the FP64 sums.
+template <class L>
+__global__ void __launch_bounds__(128, 8) k_force_fx(const __grid_constant__ DevProblem pb,
+                                                      const fx::i64* __restrict__ f,
+                                                      double* fx_o, double* fy_o, double* fz_o) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= pb.nx || y >= pb.ny) return;
+  const Nbr nb(x, y, z, pb.nx, pb.ny, pb.nz, pb.nxy);
+  const int c = nb.self();
+  double fx = 0, fy = 0, fz = 0;
+  if (pb.nd_type[c] == kSolid) {
+    const Nbr2 n2(nb, pb.nx, pb.ny, pb.nz, pb.nxy);
+    const size_t n = static_cast<size_t>(pb.n);
+    fx::i64 ax = 0, ay = 0, az = 0;
+    unsigned out = 0;
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) {  // a non-link adds zero
       const int b = L::bb(i);
-      int gx, gy, gz;
-      decompose(g, pb.nx, pb.nxy, gx, gy, gz);
-      const Nbr ng(gx, gy, gz, pb.nx, pb.ny, pb.nz, pb.nxy);
-      const C f1 = pulled(i, nb.from<L>(i));
-      const C f2 = pulled(b, ng.from<L>(b));
-      const C s = f1 + f2;
-      fx += C(L::ex(b)) * s;
-      fy += C(L::ey(b)) * s;
-      fz += C(L::ez(b)) * s;
+      const bool link = pb.nd_type[nb.to<L>(i)] == kFluid;
+      const fx::i64 v1 = link ? __ldg(f + i * n + nb.from<L>(i)) : 0;
+      const fx::i64 v2 = link ? __ldg(f + b * n + n2.to2<L>(nb, i)) : 0;
+      out |= fx::beyond_half(v1) | fx::beyond_half(v2);
+      const fx::i64 s = fx::to58(v1) + fx::to58(v2);
+      if (L::ex(b) > 0) ax += s;
+      if (L::ex(b) < 0) ax -= s;
+      if (L::ey(b) > 0) ay += s;
+      if (L::ey(b) < 0) ay -= s;
+      if (L::ez(b) > 0) az += s;
+      if (L::ez(b) < 0) az -= s;
+    }
+    if (out == 0) {
+      fx = fx::to_f64_58(ax);
+      fy = fx::to_f64_58(ay);
+      fz = fx::to_f64_58(az);
+    } else {
+      force_links_f64<L>(pb, f, nb, n2, fx, fy, fz);
     }
   }
   fx_o[c] = fx;
@@ -393,9 +478,13 @@ template <class L, int K>
 cudaError_t force_lk(const DevProblem& pb, const void* f, void* const out[3], const Launch& l) {
   using C = typename Store<K>::C;
   const dim3 g = grid_of(pb, l), b(l.bx, l.by, 1);
-  k_force_fast<L, K><<<g, b, 0, l.stream>>>(pb, f,
-                                             static_cast<C*>(out[0]), static_cast<C*>(out[1]),
-                                             static_cast<C*>(out[2]));
+  if constexpr (K == kStoreFX)
+    k_force_fx<L><<<g, b, 0, l.stream>>>(pb, static_cast<const fx::i64*>(f),
+                                         static_cast<C*>(out[0]), static_cast<C*>(out[1]),
+                                         static_cast<C*>(out[2]));
+  else
+    k_force_fast<L, K><<<g, b, 0, l.stream>>>(pb, f, static_cast<C*>(out[0]),
+                                               static_cast<C*>(out[1]), static_cast<C*>(out[2]));
   return cudaGetLastError();
 }
 
