@@ -277,6 +277,7 @@ Engine::~Engine() {
   if (h_pinned_) cudaFreeHost(h_pinned_);
   if (outputs_ready_) cudaEventDestroy(outputs_ready_);
   if (copies_done_) cudaEventDestroy(copies_done_);
+  if (macros_ready_) cudaEventDestroy(macros_ready_);
   if (copy_stream_) cudaStreamDestroy(copy_stream_);
   if (stream_) cudaStreamDestroy(stream_);
 }
@@ -307,61 +308,19 @@ Status Engine::create(const tlbm_problem& prob, const int32_t* nd_type, const in
   return Status::ok();
 }
 
-Status Engine::init(const int32_t* nd_type, const int32_t* parts, int size) {
-  q_ = lattice_q(prob_.lattice);
-  if (!q_) return Status::err(TLBM_ERR_INVALID_ARGUMENT, "Invalid Lattice Structure!");
-  if (prob_.nx < 1 || prob_.ny < 1 || prob_.nz < 1)
-    return Status::err(TLBM_ERR_FORMAT, "params.lbm: lattice dimensions must be positive");
-  n_ = static_cast<int64_t>(prob_.nx) * prob_.ny * prob_.nz;
-  if (n_ * q_ > (int64_t(1) << 40) || n_ >= (int64_t(1) << 31))
-    return Status::err(TLBM_ERR_UNSUPPORTED, "lattice too large for one device (N >= 2^31)");
-  if (prob_.nz > 65535 || prob_.ny > 65535 * 64)
-    return Status::err(TLBM_ERR_UNSUPPORTED, "nz > 65535 is not supported");
-  if (prob_.plot_freq <= 0)
-    return Status::err(TLBM_ERR_FORMAT, "params.lbm: plotFreq must be positive");
-  switch (opt_.precision) {
-    case TLBM_PREC_F64: store_ = kStoreF64; break;
-    case TLBM_PREC_F32: store_ = kStoreF32; break;
-    case TLBM_PREC_BF16: store_ = kStoreBF16; break;
-    case TLBM_PREC_F16: store_ = kStoreF16; break;
-    case TLBM_PREC_BF16M: store_ = kStoreBF16M; break;
-    default: return Status::err(TLBM_ERR_INVALID_ARGUMENT, "unknown precision option");
-  }
-  ref_arith_ = (opt_.arithmetic == TLBM_ARITH_REFERENCE);
-  if (ref_arith_ && (store_ == kStoreBF16 || store_ == kStoreF16 || store_ == kStoreBF16M))
-    return Status::err(TLBM_ERR_INVALID_ARGUMENT,
-                       "16-bit storage has no reference arithmetic; use TLBM_ARITH_FAST");
-  if ((opt_.rbgk || opt_.mrt) && ref_arith_)
-    return Status::err(TLBM_ERR_UNSUPPORTED,
-                       "the regularised and moment-space collisions have no reference arithmetic "
-                       "(the reference streams without relaxation for dynamics 2 and 3): use "
-                       "TLBM_ARITH_FAST");
-  if (opt_.mrt && opt_.mrt_ghost_rate >= 2.0f)
-    return Status::err(TLBM_ERR_INVALID_ARGUMENT, "mrt_ghost_rate must lie in (0, 2)");
-  if (opt_.closure != TLBM_CLOSURE_PARAMS)
-    return Status::err(TLBM_ERR_UNSUPPORTED, "closure option not available");
-  // FP64 in fast arithmetic: fluid nodes collide in exact fixed point (physics_fx.cuh), and the
-  // populations stay in its Q1.62 format between steps unless a moment-space collision runs
-  fx_ = store_ == kStoreF64 && !ref_arith_ && !opt_.f64_pipe &&
-        fx_collision_ok(prob_.omega, prob_.cs);
-  const bool mcoll = (opt_.rbgk && prob_.dynamics == 2) || (opt_.mrt && prob_.dynamics == 3);
-  if (fx_ && !mcoll && fx_storage_ok(prob_.omega, prob_.cs, prob_.rho_lbm)) store_ = kStoreFX;
-  sb_ = store_bytes(store_);
-  ob_ = (store_ == kStoreF64 || store_ == kStoreFX) ? 8 : 4;
-
+Status Engine::check_host_inputs(const int32_t* nd_type, const int32_t* parts, int size,
+                                 uint8_t* types) {
   // node types: the reference's codes only (python/FluidChannel.py:1386-1397); checked and
   // narrowed to bytes in chunks on several host threads, one branch-free pass per chunk (a
   // branch and an early exit per node kept the loop scalar: ~26 ms for 33.5 M nodes); a chunk
   // that holds a bad code is scanned again for its first one
-  std::unique_ptr<uint8_t[]> types(new (std::nothrow) uint8_t[static_cast<size_t>(n_)]);
-  if (!types) return Status::err(TLBM_ERR_NO_MEMORY, "out of host memory for the node types");
   {
     struct Chunk {
       int64_t bad = -1;
       bool type5 = false;
     };
     std::vector<Chunk> chunks;
-    uint8_t* const out = types.get();
+    uint8_t* const out = types;
     for_chunks(n_, &chunks, [&](int64_t begin, int64_t end, Chunk* c) {
       // codes 0, 1, 2, 3, 5; a negative code is a large unsigned value
       const auto bad_code = [](uint32_t t) { return (t > 5u) | (t == 4u); };
@@ -456,21 +415,16 @@ Status Engine::init(const int32_t* nd_type, const int32_t* parts, int size) {
     }
   }
 
+  return Status::ok();
+}
+
+Status Engine::init_device() {
   TLBM_CUDA(cudaSetDevice(opt_.device));
   TLBM_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
   launch_.stream = stream_;
-  int bx = opt_.block_x, by = opt_.block_y;
-  if (bx <= 0) bx = prob_.nx >= 128 ? 128 : 32;
-  if (by <= 0) by = std::max(1, 128 / bx);
-  if (bx * by > 128 || bx % 32 != 0)
-    return Status::err(TLBM_ERR_INVALID_ARGUMENT,
-                       "block_x must be a multiple of 32 and block_x*block_y <= 128");
-  launch_.bx = bx;
-  launch_.by = by;
 
   const size_t n = static_cast<size_t>(n_);
   TLBM_CUDA(cudaMalloc(&d_type_, n));
-  TLBM_CUDA(cudaMemcpy(d_type_, types.get(), n, cudaMemcpyHostToDevice));
   for (auto& p : d_f_) TLBM_CUDA(cudaMalloc(&p, buffer_bytes(store_, q_, n_)));
   for (auto& p : d_macro_) TLBM_CUDA(cudaMalloc(&p, n * ob_));
   for (auto& p : d_force_) TLBM_CUDA(cudaMalloc(&p, n * ob_));
@@ -483,11 +437,6 @@ Status Engine::init(const int32_t* nd_type, const int32_t* parts, int size) {
   for (auto& p : d_uyq_) {
     TLBM_CUDA(cudaMalloc(&p, 32 * 8));
     TLBM_CUDA(cudaMemsetAsync(p, 0, 32 * 8, stream_));
-  }
-  if (!identity_order_) {
-    TLBM_CUDA(cudaMalloc(&d_order_, n * sizeof(int32_t)));
-    TLBM_CUDA(cudaMemcpy(d_order_, order_.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice));
-    TLBM_CUDA(cudaMalloc(&d_stage_, n * ob_));
   }
 
   pb_.nx = prob_.nx;
@@ -510,7 +459,6 @@ Status Engine::init(const int32_t* nd_type, const int32_t* parts, int size) {
     pb_.mcoll = 1;
     pb_.ghost_omega = opt_.mrt_ghost_rate > 0.0f ? opt_.mrt_ghost_rate : 1.2;
   }
-  pb_.has_type5 = has_type5_ ? 1 : 0;
   fill_derived(pb_, q_, sb_);
   pb_.fx = fx_ ? 1 : 0;
   if (pb_.fx) fx::fill_consts(pb_.fxk, prob_.omega, prob_.cs, pb_.nu);
@@ -523,6 +471,80 @@ Status Engine::init(const int32_t* nd_type, const int32_t* parts, int size) {
   for (auto p : d_f_) {
     TLBM_CUDA(launch_init_uniform(q_, store_, pb_, p, prob_.rho_lbm, launch_));
     ++launches_;
+  }
+  return Status::ok();
+}
+
+Status Engine::init(const int32_t* nd_type, const int32_t* parts, int size) {
+  q_ = lattice_q(prob_.lattice);
+  if (!q_) return Status::err(TLBM_ERR_INVALID_ARGUMENT, "Invalid Lattice Structure!");
+  if (prob_.nx < 1 || prob_.ny < 1 || prob_.nz < 1)
+    return Status::err(TLBM_ERR_FORMAT, "params.lbm: lattice dimensions must be positive");
+  n_ = static_cast<int64_t>(prob_.nx) * prob_.ny * prob_.nz;
+  if (n_ * q_ > (int64_t(1) << 40) || n_ >= (int64_t(1) << 31))
+    return Status::err(TLBM_ERR_UNSUPPORTED, "lattice too large for one device (N >= 2^31)");
+  if (prob_.nz > 65535 || prob_.ny > 65535 * 64)
+    return Status::err(TLBM_ERR_UNSUPPORTED, "nz > 65535 is not supported");
+  if (prob_.plot_freq <= 0)
+    return Status::err(TLBM_ERR_FORMAT, "params.lbm: plotFreq must be positive");
+  switch (opt_.precision) {
+    case TLBM_PREC_F64: store_ = kStoreF64; break;
+    case TLBM_PREC_F32: store_ = kStoreF32; break;
+    case TLBM_PREC_BF16: store_ = kStoreBF16; break;
+    case TLBM_PREC_F16: store_ = kStoreF16; break;
+    case TLBM_PREC_BF16M: store_ = kStoreBF16M; break;
+    default: return Status::err(TLBM_ERR_INVALID_ARGUMENT, "unknown precision option");
+  }
+  ref_arith_ = (opt_.arithmetic == TLBM_ARITH_REFERENCE);
+  if (ref_arith_ && (store_ == kStoreBF16 || store_ == kStoreF16 || store_ == kStoreBF16M))
+    return Status::err(TLBM_ERR_INVALID_ARGUMENT,
+                       "16-bit storage has no reference arithmetic; use TLBM_ARITH_FAST");
+  if ((opt_.rbgk || opt_.mrt) && ref_arith_)
+    return Status::err(TLBM_ERR_UNSUPPORTED,
+                       "the regularised and moment-space collisions have no reference arithmetic "
+                       "(the reference streams without relaxation for dynamics 2 and 3): use "
+                       "TLBM_ARITH_FAST");
+  if (opt_.mrt && opt_.mrt_ghost_rate >= 2.0f)
+    return Status::err(TLBM_ERR_INVALID_ARGUMENT, "mrt_ghost_rate must lie in (0, 2)");
+  if (opt_.closure != TLBM_CLOSURE_PARAMS)
+    return Status::err(TLBM_ERR_UNSUPPORTED, "closure option not available");
+  // FP64 in fast arithmetic: fluid nodes collide in exact fixed point (physics_fx.cuh), and the
+  // populations stay in its Q1.62 format between steps unless a moment-space collision runs
+  fx_ = store_ == kStoreF64 && !ref_arith_ && !opt_.f64_pipe &&
+        fx_collision_ok(prob_.omega, prob_.cs);
+  const bool mcoll = (opt_.rbgk && prob_.dynamics == 2) || (opt_.mrt && prob_.dynamics == 3);
+  if (fx_ && !mcoll && fx_storage_ok(prob_.omega, prob_.cs, prob_.rho_lbm)) store_ = kStoreFX;
+  sb_ = store_bytes(store_);
+  ob_ = (store_ == kStoreF64 || store_ == kStoreFX) ? 8 : 4;
+
+  int bx = opt_.block_x, by = opt_.block_y;
+  if (bx <= 0) bx = prob_.nx >= 128 ? 128 : 32;
+  if (by <= 0) by = std::max(1, 128 / bx);
+  if (bx * by > 128 || bx % 32 != 0)
+    return Status::err(TLBM_ERR_INVALID_ARGUMENT,
+                       "block_x must be a multiple of 32 and block_x*block_y <= 128");
+  launch_.bx = bx;
+  launch_.by = by;
+
+  // The host checks of the inputs (node types, partitions, the cut size) run on a second thread
+  // while this one sets up the device (stream, buffers, the initial populations, none of which
+  // depend on them): 33.5 M nodes take ~3 ms of each.  An input error is reported before any
+  // device error, as when the checks ran first.
+  const size_t n = static_cast<size_t>(n_);
+  std::unique_ptr<uint8_t[]> types(new (std::nothrow) uint8_t[n]);
+  if (!types) return Status::err(TLBM_ERR_NO_MEMORY, "out of host memory for the node types");
+  Status host = Status::ok();
+  std::thread checker([&] { host = check_host_inputs(nd_type, parts, size, types.get()); });
+  const Status device = init_device();
+  checker.join();
+  TLBM_TRY(host);
+  TLBM_TRY(device);
+  pb_.has_type5 = has_type5_ ? 1 : 0;
+  TLBM_CUDA(cudaMemcpy(d_type_, types.get(), n, cudaMemcpyHostToDevice));
+  if (!identity_order_) {
+    TLBM_CUDA(cudaMalloc(&d_order_, n * sizeof(int32_t)));
+    TLBM_CUDA(cudaMemcpy(d_order_, order_.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice));
+    TLBM_CUDA(cudaMalloc(&d_stage_, n * ob_));
   }
   TLBM_CUDA(cudaStreamSynchronize(stream_));
   if (prob_.restart_flag) {
@@ -726,20 +748,25 @@ Status Engine::synchronize() {
   return Status::ok();
 }
 
-Status Engine::compute_outputs() {
+Status Engine::compute_outputs(cudaEvent_t macros_done) {
   if (last_src_ < 0)
     return Status::err(TLBM_ERR_INVALID_ARGUMENT, "no time step has been taken yet");
-  if (outputs_fresh_) return Status::ok();
+  if (outputs_fresh_) {
+    if (macros_done) TLBM_CUDA(cudaEventRecord(macros_done, stream_));
+    return Status::ok();
+  }
   // an asynchronous copy may still be reading the output fields
   if (copies_pending_) TLBM_CUDA(cudaStreamWaitEvent(stream_, copies_done_, 0));
   // macroscopic values of the last step, recomputed from its (untouched) pull source
-  if (ref_arith_) {
+  if (ref_arith_)
     TLBM_CUDA(launch_macros_ref(q_, sb_, pb_, d_f_[last_src_], d_macro_, launch_));
-    TLBM_CUDA(launch_force_ref(q_, sb_, pb_, d_f_[last_dst_], d_force_, launch_));
-  } else {
+  else
     TLBM_CUDA(launch_macros_fast(q_, store_, pb_, d_f_[last_src_], d_macro_, launch_));
+  if (macros_done) TLBM_CUDA(cudaEventRecord(macros_done, stream_));
+  if (ref_arith_)
+    TLBM_CUDA(launch_force_ref(q_, sb_, pb_, d_f_[last_dst_], d_force_, launch_));
+  else
     TLBM_CUDA(launch_force_fast(q_, store_, pb_, d_f_[last_dst_], d_force_, launch_));
-  }
   launches_ += 2;
   outputs_fresh_ = true;
   return Status::ok();
@@ -883,14 +910,15 @@ Status Engine::copy_force(void* fx, void* fy, void* fz) {
 Status Engine::copy_outputs_async(void* const host[7]) {
   TraceRange trace("tlbm_copy_outputs_async");
   TLBM_CUDA(cudaSetDevice(opt_.device));
-  TLBM_TRY(compute_outputs());
-  if (!copy_stream_) {  // all three or none
+  if (!copy_stream_) {  // all four or none
     cudaStream_t cs = nullptr;
-    cudaEvent_t ready = nullptr, done = nullptr;
+    cudaEvent_t ready = nullptr, done = nullptr, macros = nullptr;
     cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ready, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&macros, cudaEventDisableTiming);
     if (e != cudaSuccess) {
+      if (macros) cudaEventDestroy(macros);
       if (done) cudaEventDestroy(done);
       if (ready) cudaEventDestroy(ready);
       if (cs) cudaStreamDestroy(cs);
@@ -899,41 +927,46 @@ Status Engine::copy_outputs_async(void* const host[7]) {
     copy_stream_ = cs;
     outputs_ready_ = ready;
     copies_done_ = done;
+    macros_ready_ = macros;
   }
+  TLBM_TRY(compute_outputs(macros_ready_));
   TLBM_CUDA(cudaEventRecord(outputs_ready_, stream_));
-  TLBM_CUDA(cudaStreamWaitEvent(copy_stream_, outputs_ready_, 0));
   const size_t bytes = static_cast<size_t>(n_) * ob_;
   const void* dev[7] = {d_macro_[0], d_macro_[1], d_macro_[2], d_macro_[3],
                         d_force_[0], d_force_[1], d_force_[2]};
   // Page-locked destinations are written by a copy kernel on the copy stream: on GB300 its
   // stores reach page-locked host memory at the copy engines' rate (~190 GB/s), and some
   // copy-engine transfers issued from an application process ran at ~16 GB/s.  Other
-  // destinations take cudaMemcpyAsync.
-  const void* ksrc[7];
-  void* kdst[7];
-  int nk = 0;
-  for (int k = 0; k < 7; ++k) {
-    if (!host[k]) continue;
-    cudaPointerAttributes at{};
-    const bool pinned = cudaPointerGetAttributes(&at, host[k]) == cudaSuccess &&
-                        at.type == cudaMemoryTypeHost &&
-                        reinterpret_cast<uintptr_t>(host[k]) % 16 == 0 && bytes % 16 == 0;
-    cudaGetLastError();  // a pageable pointer can leave an error state behind
-    if (pinned) {
-      ksrc[nk] = dev[k];
-      kdst[nk] = at.devicePointer ? at.devicePointer : host[k];
-      ++nk;
-    } else {
-      TLBM_CUDA(cudaMemcpyAsync(host[k], dev[k], bytes, cudaMemcpyDeviceToHost, copy_stream_));
+  // destinations take cudaMemcpyAsync.  ux..rho start as soon as they are computed, while the
+  // force kernel runs; Fx..Fz follow it.
+  for (int group = 0; group < 2; ++group) {
+    TLBM_CUDA(cudaStreamWaitEvent(copy_stream_, group == 0 ? macros_ready_ : outputs_ready_, 0));
+    const void* ksrc[4];
+    void* kdst[4];
+    int nk = 0;
+    for (int k = group == 0 ? 0 : 4; k < (group == 0 ? 4 : 7); ++k) {
+      if (!host[k]) continue;
+      cudaPointerAttributes at{};
+      const bool pinned = cudaPointerGetAttributes(&at, host[k]) == cudaSuccess &&
+                          at.type == cudaMemoryTypeHost &&
+                          reinterpret_cast<uintptr_t>(host[k]) % 16 == 0 && bytes % 16 == 0;
+      cudaGetLastError();  // a pageable pointer can leave an error state behind
+      if (pinned) {
+        ksrc[nk] = dev[k];
+        kdst[nk] = at.devicePointer ? at.devicePointer : host[k];
+        ++nk;
+      } else {
+        TLBM_CUDA(cudaMemcpyAsync(host[k], dev[k], bytes, cudaMemcpyDeviceToHost, copy_stream_));
+      }
     }
-  }
-  if (nk > 0) {
-    if (sms_ == 0) TLBM_CUDA(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount,
-                                                    opt_.device));
-    Launch cl = launch_;
-    cl.stream = copy_stream_;
-    TLBM_CUDA(launch_copy_words(ksrc, kdst, nk, bytes, 2 * sms_, cl));
-    ++launches_;
+    if (nk > 0) {
+      if (sms_ == 0) TLBM_CUDA(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount,
+                                                      opt_.device));
+      Launch cl = launch_;
+      cl.stream = copy_stream_;
+      TLBM_CUDA(launch_copy_words(ksrc, kdst, nk, bytes, 2 * sms_, cl));
+      ++launches_;
+    }
   }
   TLBM_CUDA(cudaEventRecord(copies_done_, copy_stream_));
   copies_pending_ = true;

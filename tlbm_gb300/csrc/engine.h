@@ -81,9 +81,16 @@ class Engine {
  private:
   Engine() = default;
   Status init(const int32_t* nd_type, const int32_t* parts, int size);
+  // init's two halves, run concurrently: the host checks of the node types (narrowed into
+  // `types`) and partitions, and the device setup that does not depend on them
+  Status check_host_inputs(const int32_t* nd_type, const int32_t* parts, int size,
+                           uint8_t* types);
+  Status init_device();
   Status check(cudaError_t e, const char* what);
   Status enqueue_step(int is_even);
-  Status compute_outputs();
+  // the output fields of the last step (no-op while fresh); macros_done, if given, is recorded
+  // on the stream once ux..rho are ready
+  Status compute_outputs(cudaEvent_t macros_done = nullptr);
   Status fetch(const void* dev, void* host);  // one field, global order
   Status write_field(const std::string& name, const void* dev);
   Status build_graph(int parity);
@@ -106,10 +113,11 @@ class Engine {
   DevProblem pb_{};
   Launch launch_{};
   cudaStream_t stream_ = nullptr;
-  // copy_outputs_async: copies on copy_stream_ after outputs_ready_; the next recomputation of
-  // the output fields waits for copies_done_
+  // copy_outputs_async: copies on copy_stream_, ux..rho after macros_ready_ (while the force
+  // kernel runs), Fx..Fz after outputs_ready_; the next recomputation of the output fields
+  // waits for copies_done_
   cudaStream_t copy_stream_ = nullptr;
-  cudaEvent_t outputs_ready_ = nullptr, copies_done_ = nullptr;
+  cudaEvent_t outputs_ready_ = nullptr, copies_done_ = nullptr, macros_ready_ = nullptr;
   bool copies_pending_ = false;
 
   uint8_t* d_type_ = nullptr;
