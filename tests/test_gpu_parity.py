@@ -510,6 +510,37 @@ def test_async_output_copies_overlap_later_steps():
     b.close()
 
 
+def test_q62_outputs_take_fp64_code_for_non_finite_nodes():
+    """Q1.62 storage holds a non-finite population as its NaN marker. The step, the field
+    kernel and the force kernel send such nodes to their FP64 code. A NaN density restarted
+    into the fluid node just below the sphere spreads for two steps. ux..rho and the force are
+    then NaN exactly where the FP64-arithmetic run (double storage) has NaN, and agree with it
+    elsewhere."""
+    g = G.sphere_in_box(12, 10, 24, 3, 6, 5, 8)
+    p = G.params_lattice_units(g, "D3Q19", 0.04, 30.0, 6.0, 12, cs=0.1)
+    n = g.num_nodes
+    c = 6 + 5 * g.nx + 5 * g.nx * g.ny  # (6, 5, 5): fluid, the sphere at z = 6 above it
+    assert g.nd_type[c] == 0 and g.nd_type[c + g.nx * g.ny] == 1
+    ux, uy = np.zeros(n, np.float32), np.zeros(n, np.float32)
+    uz, rho = np.full(n, 0.04, np.float32), np.ones(n, np.float32)
+    rho[c] = np.nan
+    out = []
+    for arith in FAST64:
+        part = T.TLBMPartition.from_arrays(T.problem_from_params(p), g.nd_type, precision="f64",
+                                           arithmetic=arith)
+        part.load_restart(ux, uy, uz, rho)
+        part.run(0, 2)
+        out.append(part.macros() + part.force())
+        part.close()
+    fast, fp64 = out
+    names = ["ux", "uy", "uz", "rho", "Fx", "Fy", "Fz"]
+    for name, a, b in zip(names, fast, fp64):
+        nan = np.isnan(b)
+        assert np.array_equal(np.isnan(a), nan), name
+        assert nan.any(), name  # the NaN reached this field
+        assert rel_inf(a[~nan], b[~nan]) <= 1e-12, name
+
+
 @pytest.mark.parametrize("arith", FAST64)
 @pytest.mark.parametrize("q,dims", [(19, (1, 5, 12)), (19, (6, 1, 12)), (27, (1, 1, 10)),
                                     (15, (2, 3, 9)), (19, (33, 2, 7))])
