@@ -91,8 +91,10 @@ class Engine {
   // the output fields of the last step (no-op while fresh); macros_done, if given, is recorded
   // on the stream once ux..rho are ready
   Status compute_outputs(cudaEvent_t macros_done = nullptr);
-  Status fetch(const void* dev, void* host);  // one field, global order
-  Status write_field(const std::string& name, const void* dev);
+  // one field in global order into host memory, on the stream (wait: synchronize it)
+  Status fetch(const void* dev, void* host, bool wait = true);
+  // the dump files names[0..k) of the fields dev[0..k), k <= 7, written in parallel
+  Status write_fields(const std::string* names, const void* const* dev, int k);
   Status build_graph(int parity);
 
   tlbm_problem prob_{};
