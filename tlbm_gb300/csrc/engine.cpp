@@ -21,6 +21,7 @@
 #include <cstring>
 #include <fstream>
 #include <memory>
+#include <new>
 #include <sstream>
 #include <system_error>
 #include <thread>
@@ -46,8 +47,14 @@ void for_chunks(int64_t n, std::vector<State>* states, Fn fn) {
   states->assign(static_cast<size_t>(t), State{});
   const int64_t per = (n + t - 1) / t;
   std::vector<std::thread> pool;
-  for (int64_t k = 1; k < t; ++k)
-    pool.emplace_back([&, k] { fn(k * per, std::min(n, (k + 1) * per), &(*states)[k]); });
+  for (int64_t k = 1; k < t; ++k) {
+    auto chunk = [&, k] { fn(k * per, std::min(n, (k + 1) * per), &(*states)[k]); };
+    try {
+      pool.emplace_back(chunk);
+    } catch (const std::system_error&) {
+      chunk();  // no thread to be had: this chunk in turn
+    }
+  }
   fn(0, std::min(n, per), &(*states)[0]);
   for (auto& th : pool) th.join();
 }
@@ -535,9 +542,21 @@ Status Engine::init(const int32_t* nd_type, const int32_t* parts, int size) {
   std::unique_ptr<uint8_t[]> types(new (std::nothrow) uint8_t[n]);
   if (!types) return Status::err(TLBM_ERR_NO_MEMORY, "out of host memory for the node types");
   Status host = Status::ok();
-  std::thread checker([&] { host = check_host_inputs(nd_type, parts, size, types.get()); });
+  auto checks = [&] {  // no exception may leave a thread
+    try {
+      host = check_host_inputs(nd_type, parts, size, types.get());
+    } catch (const std::bad_alloc&) {
+      host = Status::err(TLBM_ERR_NO_MEMORY, "out of host memory checking the inputs");
+    }
+  };
+  std::thread checker;
+  try {
+    checker = std::thread(checks);
+  } catch (const std::system_error&) {
+    checks();  // no thread to be had: the checks first, as before
+  }
   const Status device = init_device();
-  checker.join();
+  if (checker.joinable()) checker.join();
   TLBM_TRY(host);
   TLBM_TRY(device);
   pb_.has_type5 = has_type5_ ? 1 : 0;
@@ -799,8 +818,12 @@ Status Engine::write_fields(const std::string* names, const void* const* dev, in
   for (int j = 0; j < k; ++j) TLBM_TRY(fetch(dev[j], base + j * bytes, false));
   TLBM_CUDA(cudaStreamSynchronize(stream_));
   std::vector<Status> st(static_cast<size_t>(k));
-  auto write_one = [&](int j) {
-    st[j] = write_at(workdir_ + "/" + names[j], base + j * bytes, bytes, 0);
+  auto write_one = [&](int j) {  // no exception may leave a thread
+    try {
+      st[j] = write_at(workdir_ + "/" + names[j], base + j * bytes, bytes, 0);
+    } catch (const std::bad_alloc&) {
+      st[j] = Status::err(TLBM_ERR_NO_MEMORY, "out of host memory writing a dump file");
+    }
   };
   std::vector<std::thread> pool;
   for (int j = 1; j < k; ++j) {
