@@ -124,6 +124,13 @@ def test_ndtype_bad_code_lowest_node_named(lib):
     nd[1_234_567] = 0
     st, msg = _create(_problem(nx, ny, nz), nd, precision="f64")
     assert st == T.ERR_OUT_OF_RANGE and "node 2500000 " in msg and "type 7" in msg
+    # two bad codes in one chunk ([2^20, 2^21)): its branch-free pass only flags it, and the
+    # rescan names the first
+    nd[2_500_000] = nd[3_900_000] = 0
+    nd[1_100_000] = 6
+    nd[1_060_000] = 4
+    st, msg = _create(_problem(nx, ny, nz), nd, precision="f64")
+    assert st == T.ERR_OUT_OF_RANGE and "node 1060000 " in msg and "type 4" in msg
 
 
 def test_parts_beyond_job_size(lib, tmp_path):
