@@ -332,9 +332,9 @@ __device__ __noinline__ void force_links_f64(const DevProblem& pb, const void* f
 // Q1.62 storage: the link sums accumulate as integers (each value rounded once to 2^-58; Q5.58
 // holds the 2 (Q - 1) values in [-1/2, 1/2) a node can gather), three conversions per node.  The
 // work sits in the warps that hold solid surface nodes and is bound by load latency: 64 registers
-// (eight resident blocks per SM, against three at the 138 the FP64 form of the sums takes) and
-// predicated loads that issue without waiting on each link's type test.  A value outside the
-// range (the stored NaN included) sends the node to the FP64 sums.
+// (eight resident blocks per SM, against three at the 138 the same sums took with the FP64
+// fallback inline) and predicated loads that issue without waiting on each link's type test.  A
+// value outside the range (the stored NaN included) sends the node to the FP64 sums.
 template <class L>
 __global__ void __launch_bounds__(128, 8) k_force_fx(const __grid_constant__ DevProblem pb,
                                                       const fx::i64* __restrict__ f,
