@@ -562,13 +562,14 @@ def e2e(args, g, p, dist, plot_every=100):
     return {
         "value": round(n * steps * dist.world / dt / 1e6, 2),
         "unit": "MLUPS",
-        "h2d_bytes_per_step": round(n * 4 / steps),
+        "h2d_bytes_per_step": round(n / steps),  # the node types, narrowed to bytes on the host
         "d2h_bytes_per_step": round(d2h / steps),
         "seconds": {"total": round(dt, 4), "create": round(t_create, 4)},
         "definition": "the reference's Estimated LPU/s (src/tLBM.cpp:69-73: nodes x steps over "
                       "the time from construction to the end, dumps included), with the dumps "
                       "read back to host memory instead of written to files",
-        "includes": "lattice upload (int32 node types, once per run) + %d tlbm_step calls + "
+        "includes": "construction (the caller's int32 node types checked and narrowed to "
+                    "bytes on the host, uploaded once per run) + %d tlbm_step calls + "
                     "write_data fields (7 x %d values) read back after every %dth step and after "
                     "the last one into page-locked host buffers, each copy overlapping the steps "
                     "after it" % (steps, n, plot_every),
